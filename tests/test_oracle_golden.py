@@ -1,0 +1,75 @@
+"""Pins the CPU oracle to the reference's own outputs (no GPU needed)."""
+
+import numpy as np
+import pytest
+
+from oracle import seemps_oracle as so
+from tests.golden_cases import CASE_NAMES, load_case, run_oracle, truncation_cases
+
+
+@pytest.mark.parametrize("chunk", range(4))
+def test_truncation_known_answers(chunk):
+    """Every reference truncation case: same kept size, bit-identical error."""
+    cases = truncation_cases()
+    for s, c in cases[chunk::4]:
+        st = so.Strategy(method=c["method"], tolerance=c["tol"], max_bond_dimension=c["maxb"])
+        assert st.method == c["effective_method"]
+        size, err = so.truncate(s, st)
+        assert size == c["size"], (c, size)
+        if st.method == so.Truncation.RELATIVE_NORM_SQUARED_ERROR:
+            # prefix sums are stored one by one: the order is fixed, bit-exact
+            assert err == c["err"], (c, err)
+        else:
+            # the reference core is built with -ffast-math, which may reassociate
+            # the plain sum of dropped s^2 of the singular-value rules
+            assert abs(err - c["err"]) <= 8 * np.finfo(float).eps * abs(c["err"]), (c, err)
+
+
+def test_reference_inline_vectors():
+    """tests/test_truncate/test_truncation.py:83-147 of the reference, restated."""
+    s = np.array([1.0, 0.1, 0.01, 0.001, 0.0001])
+    expected = [1.01010100e-02, 1.01010000e-04, 1.01000000e-06, 9.99999994e-09, 0.0]
+    for k, tol in enumerate([0.1, 1e-3, 1e-5, 1e-7, 1e-9]):
+        st = so.Strategy(method=so.Truncation.RELATIVE_NORM_SQUARED_ERROR, tolerance=tol)
+        size, err = so.truncate(s, st)
+        assert size == k + 1
+        assert abs(err - expected[k]) < 1e-7
+
+
+def test_strategy_validation():
+    with pytest.raises(AssertionError):
+        so.Strategy(tolerance=-1.0)
+    with pytest.raises(AssertionError):
+        so.Strategy(tolerance=1.0)
+    with pytest.raises(AssertionError):
+        so.Strategy(max_bond_dimension=0)
+    with pytest.raises(AssertionError):
+        so.Strategy(max_sweeps=-1)
+    assert so.Strategy(tolerance=0.0).method == so.Truncation.ABSOLUTE_SINGULAR_VALUE
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_oracle_matches_reference_run(name):
+    p, mps, mpo, g, same = load_case(name)
+    if not same:
+        pytest.skip("this numpy regenerates different seeded inputs than the fixture's")
+    rec = so.Recorder()
+    res, target = run_oracle(p, mps, mpo, rec)
+    bonds = [A.shape[0] for A in res.tensors] + [res.tensors[-1].shape[-1]]
+    assert bonds == g["bonds"].tolist()
+    assert res.center == int(g["center"])
+    # every split: identical kept rank, singular values within 1e-10 of s_max
+    assert [sp.rank for sp in rec.splits] == g["split_rank"].tolist()
+    for sp, s_ref in zip(rec.splits, g["splits_s"]):
+        assert len(sp.s) == len(s_ref)
+        smax = max(float(s_ref[0]), 1e-300)
+        assert np.max(np.abs(sp.s - s_ref)) <= 1e-10 * smax
+    # error bound: its square is the stable quantity (see make_golden.py)
+    e1, e2 = res.error ** 2, float(g["error"]) ** 2
+    assert abs(e1 - e2) <= 1e-13 + 1e-8 * e2
+    n2 = so.norm_squared(res.tensors)
+    assert abs(n2 - float(g["norm2"])) <= 1e-10 * float(g["norm2"])
+    if "vector" in g:
+        v = so.to_vector(res.tensors)
+        ref = g["vector"]
+        assert np.linalg.norm(v - ref) <= 1e-9 * np.linalg.norm(ref)
