@@ -1,0 +1,186 @@
+/*
+ * seemps_gb300.h — C ABI of the GB300 (sm_103a) MPO·MPS + simplify path.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*, may be NULL for the legacy stream) and returns an int
+ * status (SM_OK on success).  No entry point takes or returns a PyTorch type.
+ * Tensors are C-ordered (row-major):
+ *   MPS site  A[a, i, b]        (reference state/mps.py:23-38)
+ *   MPO site  O[a, i, j, b]     (reference operators/mpo.py:51-54)
+ * dtype SM_FLOAT64 is double; SM_COMPLEX128 is interleaved (re, im) doubles,
+ * the byte layout of numpy/torch complex128.
+ *
+ * Status codes map onto the exceptions the reference raises:
+ *   SM_ERR_VALUE     -> ValueError     (bad shapes, e.g. cython/environments.pxi:11-17)
+ *   SM_ERR_STRATEGY  -> AssertionError (invalid Strategy, cython/truncation.pxi:103-131)
+ *   SM_ERR_LINALG    -> LinAlgError    (SVD did not converge, cython/svd.pxi:80-83)
+ *   SM_ERR_CUDA, SM_ERR_TIMEOUT, SM_ERR_NOMEM -> RuntimeError
+ * sm_last_error() returns the message of the last failure on this thread.
+ */
+#ifndef SEEMPS_GB300_H
+#define SEEMPS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SM_ABI_VERSION 1
+
+enum {
+  SM_OK = 0,
+  SM_ERR_VALUE = 1,
+  SM_ERR_CUDA = 2,
+  SM_ERR_LINALG = 3,
+  SM_ERR_TIMEOUT = 4,
+  SM_ERR_STRATEGY = 5,
+  SM_ERR_NOMEM = 6,
+};
+
+enum { SM_FLOAT64 = 0, SM_COMPLEX128 = 1 };
+enum { SM_OP_N = 0, SM_OP_T = 1, SM_OP_C = 2 }; /* GemmOrder: cython/gemm.pxi:17-20 */
+
+/* Truncation / Simplification codes: cython/truncation.pxi:4-16 */
+enum {
+  SM_DO_NOT_TRUNCATE = 0,
+  SM_RELATIVE_SINGULAR_VALUE = 1,
+  SM_RELATIVE_NORM_SQUARED_ERROR = 2,
+  SM_ABSOLUTE_SINGULAR_VALUE = 3,
+};
+enum {
+  SM_DO_NOT_SIMPLIFY = 0,
+  SM_CANONICAL_FORM = 1,
+  SM_VARIATIONAL = 2,
+  SM_VARIATIONAL_EXACT_GUESS = 3,
+};
+
+/* Plain-data mirror of the reference cdef class Strategy (cython/truncation.pxi:66-100). */
+typedef struct sm_strategy {
+  int32_t method;
+  int32_t max_bond_dimension;
+  double tolerance;
+  double simplification_tolerance;
+  int32_t normalize;
+  int32_t simplify;
+  int32_t max_sweeps;
+  int32_t reserved;
+} sm_strategy;
+
+/* Outcome of a simplify / apply call (state/simplification.py:104-142). */
+typedef struct sm_simplify_report {
+  double error;           /* total error bound written into the result (mps._error) */
+  double norm_state_sqr;  /* |state|^2 used by the stop rule */
+  double norm_mps_sqr;    /* |result|^2 before optional normalisation */
+  double last_err;        /* final sweep estimate err = 2|1 - Re<mps|state>/..| */
+  int32_t sweeps;         /* sweeps actually run */
+  int32_t center;         /* orthogonality centre of the result */
+  int32_t splits;         /* number of SVD splits performed (canonical + two-site) */
+  int32_t zero_state;     /* 1 when |state|^2 == 0 and the zero state was returned */
+  double sweep_err[64];   /* per-sweep err estimates (first 64) */
+} sm_simplify_report;
+
+/* ---- library / context ------------------------------------------------- */
+int sm_abi_version(void);
+const char* sm_last_error(void);
+/* A context owns scratch device memory and pinned host words; one per thread. */
+int sm_ctx_create(void** ctx, int device);
+int sm_ctx_destroy(void* ctx);
+
+/* ---- kernel table (replaces seemps.cython, cython/__init__.py:25-54) ----- */
+
+/* destructively_truncate_vector (cython/truncation.pxi:329-334): s_dev holds n
+ * descending singular values on the device; returns the kept size and the
+ * squared discarded weight with the reference's exact comparisons. */
+int sm_truncate(void* ctx, const double* s_dev, int n, const sm_strategy* st,
+                int* rank, double* err2, void* stream);
+
+/* _gemm (cython/gemm.pxi:21-122) in row-major form: C[M,N] = op(A) op(B). */
+int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
+            const void* A, int lda, const void* B, int ldb, void* C, int ldc,
+            void* stream);
+
+/* _destructive_svd (cython/svd.pxi:17-83): economy SVD A[m,n] = U diag(s) Vt,
+ * s descending; U is m x r, Vt is r x n, r = min(m, n).  A is not modified. */
+int sm_svd(void* ctx, int dtype, const void* A, int m, int n, void* U, double* s,
+           void* Vt, void* stream);
+
+/* _left_orth_2site (cython/schmidt.pxi:123-147): AA[a,d1,d2,b] ->
+ * U[a,d1,D] (left isometry) and SV[D,d2,b].  Buffers U and SV must hold
+ * a*d1*r and r*d2*b elements (r = min(a*d1, d2*b)); outputs are written
+ * contiguously for the kept D.  *err = sqrt(discarded weight). */
+int sm_left_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int d2,
+                       int b, const sm_strategy* st, void* U, void* SV, int* D,
+                       double* err, void* stream);
+/* _right_orth_2site (cython/schmidt.pxi:150-174): -> US[a,d1,D], V[D,d2,b]. */
+int sm_right_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int d2,
+                        int b, const sm_strategy* st, void* US, void* V, int* D,
+                        double* err, void* stream);
+
+/* _update_left_environment (cython/environments.pxi:10-37):
+ * out[n,k] = sum conj(B[l,j,n]) rho[l,i] A[i,j,k]; B is (l,j,n), A is (i,j,k). */
+int sm_update_left_environment(void* ctx, int dtype, const void* B, int l, int j,
+                               int n, const void* A, int i, int k, const void* rho,
+                               void* out, void* stream);
+/* _update_right_environment (cython/environments.pxi:39-67):
+ * out[i,l] = sum A[i,j,k] rho[k,n] conj(B[l,j,n]). */
+int sm_update_right_environment(void* ctx, int dtype, const void* B, int l, int j,
+                                int n, const void* A, int i, int k, const void* rho,
+                                void* out, void* stream);
+
+/* _mpo_multiply_tensor (operators/mpo.py:26-45):
+ * C[c*a, i, d*b] = sum_j B[c,j,d] O[a,i,j,b]. */
+int sm_mpo_multiply_tensor(void* ctx, int dtype, const void* O, int a, int i, int j,
+                           int b, const void* B, int c, int d, void* C, void* stream);
+
+/* scprod (cython/environments.pxi:87-118) of two MPS with L sites; site
+ * pointers and bonds (L+1 each) per state; result written to out[0] (and the
+ * imaginary part to out[1] for complex). */
+int sm_scprod(void* ctx, int dtype, int L, const int* phys, const int* bra_bonds,
+              const void* const* bra, const int* ket_bonds, const void* const* ket,
+              double* out, void* stream);
+
+/* _canonicalize (cython/schmidt.pxi:109-120) in place: sites[i] buffers must
+ * hold cap[i] elements; bonds (L+1) are updated; *err = summed sqrt errors. */
+int sm_canonicalize(void* ctx, int dtype, int L, const int* phys, int* bonds,
+                    void* const* sites, const int64_t* cap, int center,
+                    const sm_strategy* st, double* err, void* stream);
+
+/* simplify / simplify_mps_sum (state/simplification.py:32-280) of
+ * sum_t w_t |psi_t> (nterms >= 1; weights as (re, im) pairs).  ket_bonds holds
+ * nterms*(L+1) ints, ket_sites nterms*L pointers, term_errors the nterms
+ * accumulated errors of the input states (MPS._error).  The result is written
+ * into out_sites[i] (capacity out_cap[i] elements) with bonds out_bonds (L+1);
+ * out_cap comes from sm_simplify_bond_caps.  A single state (nterms == 1) uses
+ * its weight as given by the caller (1.0 for simplify(MPS)). */
+int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms,
+                const double* weights, const int* ket_bonds,
+                const void* const* ket_sites, const double* term_errors,
+                const sm_strategy* st, int direction, void* const* out_sites,
+                const int64_t* out_cap, int* out_bonds, sm_simplify_report* rep,
+                void* stream);
+
+/* Upper bound on the bond dimensions a simplify of these kets can produce:
+ * min(max_bond_dimension, summed ket bond); fills cap_bonds (L+1). */
+int sm_simplify_bond_caps(int L, const int* phys, int nterms, const int* ket_bonds,
+                          const sm_strategy* st, int* cap_bonds);
+
+/* Split trace.  While enabled, every SVD split run by this context appends a
+ * record: its singular values (all of them, descending), the kept rank and
+ * the squared discarded weight.  sm_trace_enable clears the trace.
+ * sm_trace_read with null buffers returns the record count and the total
+ * number of singular values; with buffers it copies them out. */
+int sm_trace_enable(void* ctx, int on);
+int sm_trace_read(void* ctx, int* count, int64_t* total_s, int* ranks, int* lens,
+                  double* err2, double* svals);
+
+/* Device FP64 throughput probe: runs `iters` dependent FMA chains per thread
+ * over the given grid and reports elapsed milliseconds (CUDA events). */
+int sm_probe_fp64(void* ctx, int blocks, int threads, int iters, double* ms,
+                  double* flops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEEMPS_GB300_H */

@@ -1,0 +1,209 @@
+"""ctypes binding of libseemps_gb300.so (the C ABI declared in include/seemps_gb300.h).
+
+There is no CPU fallback: importing the compute entry points without the
+built library, or calling them without a CUDA device, raises immediately.
+Status codes are translated into the exceptions the reference raises
+(ValueError, AssertionError, numpy.linalg.LinAlgError, RuntimeError).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libseemps_gb300.so")
+
+SM_OK, SM_ERR_VALUE, SM_ERR_CUDA, SM_ERR_LINALG, SM_ERR_TIMEOUT, SM_ERR_STRATEGY, SM_ERR_NOMEM = range(7)
+SM_FLOAT64, SM_COMPLEX128 = 0, 1
+SM_OP_N, SM_OP_T, SM_OP_C = 0, 1, 2
+
+
+class sm_strategy(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32),
+        ("max_bond_dimension", C.c_int32),
+        ("tolerance", C.c_double),
+        ("simplification_tolerance", C.c_double),
+        ("normalize", C.c_int32),
+        ("simplify", C.c_int32),
+        ("max_sweeps", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class sm_simplify_report(C.Structure):
+    _fields_ = [
+        ("error", C.c_double),
+        ("norm_state_sqr", C.c_double),
+        ("norm_mps_sqr", C.c_double),
+        ("last_err", C.c_double),
+        ("sweeps", C.c_int32),
+        ("center", C.c_int32),
+        ("splits", C.c_int32),
+        ("zero_state", C.c_int32),
+        ("sweep_err", C.c_double * 64),
+    ]
+
+
+vp = C.c_void_p
+ip = C.POINTER(C.c_int)
+dp = C.POINTER(C.c_double)
+i64p = C.POINTER(C.c_int64)
+stp = C.POINTER(sm_strategy)
+
+# name -> (restype, argtypes); every symbol declared in include/seemps_gb300.h
+SIGNATURES = {
+    "sm_abi_version": (C.c_int, []),
+    "sm_last_error": (C.c_char_p, []),
+    "sm_ctx_create": (C.c_int, [C.POINTER(vp), C.c_int]),
+    "sm_ctx_destroy": (C.c_int, [vp]),
+    "sm_truncate": (C.c_int, [vp, vp, C.c_int, stp, ip, dp, vp]),
+    "sm_gemm": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int,
+                          vp, C.c_int, vp, C.c_int, vp]),
+    "sm_svd": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp]),
+    "sm_left_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,
+                                     vp, ip, dp, vp]),
+    "sm_right_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,
+                                      vp, ip, dp, vp]),
+    "sm_update_left_environment": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, C.c_int,
+                                             C.c_int, vp, vp, vp]),
+    "sm_update_right_environment": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp,
+                                              C.c_int, C.c_int, vp, vp, vp]),
+    "sm_mpo_multiply_tensor": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp,
+                                         C.c_int, C.c_int, vp, vp]),
+    "sm_scprod": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(vp), ip, C.POINTER(vp), dp, vp]),
+    "sm_canonicalize": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(vp), i64p, C.c_int, stp,
+                                  dp, vp]),
+    "sm_simplify": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, dp, ip, C.POINTER(vp), dp, stp,
+                              C.c_int, C.POINTER(vp), i64p, ip, C.POINTER(sm_simplify_report), vp]),
+    "sm_simplify_bond_caps": (C.c_int, [C.c_int, ip, C.c_int, ip, stp, ip]),
+    "sm_trace_enable": (C.c_int, [vp, C.c_int]),
+    "sm_trace_read": (C.c_int, [vp, ip, i64p, ip, ip, dp, dp]),
+    "sm_probe_fp64": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, vp]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path: str | None = None):
+    """Load the shared library (built by seemps2_gb300._build); raises if absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise ImportError(
+                f"{p} is missing: build it with `python -m seemps2_gb300._build` "
+                "(there is no CPU fallback for the MPO/MPS kernels)")
+        lib = C.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return lib
+
+
+class LinAlgError(np.linalg.LinAlgError):
+    pass
+
+
+def check(status: int):
+    if status == SM_OK:
+        return
+    msg = load().sm_last_error().decode(errors="replace")
+    if status == SM_ERR_VALUE:
+        raise ValueError(msg)
+    if status == SM_ERR_STRATEGY:
+        raise AssertionError(msg)
+    if status == SM_ERR_LINALG:
+        raise LinAlgError(msg)
+    raise RuntimeError(f"seemps_gb300 status {status}: {msg}")
+
+
+_ctx_local = threading.local()
+
+
+def context(device: int = 0) -> int:
+    """Per-thread, per-device library context (scratch memory and pinned words)."""
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("seemps2_gb300 needs a CUDA device (sm_103a); none is available")
+    cache = getattr(_ctx_local, "ctx", None)
+    if cache is None:
+        cache = _ctx_local.ctx = {}
+    if device not in cache:
+        h = vp()
+        lib = load()
+        torch.cuda.init()
+        with torch.cuda.device(device):
+            check(lib.sm_ctx_create(C.byref(h), device))
+        cache[device] = h
+    return cache[device]
+
+
+def stream_handle(device=None):
+    import torch
+
+    return vp(torch.cuda.current_stream(device).cuda_stream)
+
+
+def ptr(t) -> vp:
+    return vp(t.data_ptr())
+
+
+def ptr_array(ts) -> C.Array:
+    arr = (vp * len(ts))()
+    for k, t in enumerate(ts):
+        arr[k] = t.data_ptr()
+    return arr
+
+
+def int_array(xs) -> C.Array:
+    return (C.c_int * len(xs))(*[int(x) for x in xs])
+
+
+def i64_array(xs) -> C.Array:
+    return (C.c_int64 * len(xs))(*[int(x) for x in xs])
+
+
+def dbl_array(xs) -> C.Array:
+    return (C.c_double * len(xs))(*[float(x) for x in xs])
+
+
+class SplitTrace:
+    """Context manager recording every SVD split (singular values, rank, err^2)."""
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.ranks, self.err2, self.s = [], [], []
+
+    def __enter__(self):
+        check(load().sm_trace_enable(context(self.device), 1))
+        return self
+
+    def __exit__(self, *exc):
+        lib = load()
+        ctx = context(self.device)
+        n = C.c_int()
+        tot = C.c_int64()
+        check(lib.sm_trace_read(ctx, C.byref(n), C.byref(tot), None, None, None, None))
+        ranks = (C.c_int * max(1, n.value))()
+        lens = (C.c_int * max(1, n.value))()
+        err2 = (C.c_double * max(1, n.value))()
+        sv = (C.c_double * max(1, tot.value))()
+        check(lib.sm_trace_read(ctx, None, None, ranks, lens, err2, sv))
+        check(lib.sm_trace_enable(ctx, 0))
+        self.ranks = [ranks[k] for k in range(n.value)]
+        self.err2 = [err2[k] for k in range(n.value)]
+        allv = np.frombuffer(sv, dtype=np.float64, count=tot.value).copy()
+        offs = np.concatenate([[0], np.cumsum([lens[k] for k in range(n.value)])]).astype(int)
+        self.s = [allv[offs[k]:offs[k + 1]] for k in range(n.value)]
+        return False

@@ -1,0 +1,400 @@
+// extern "C" boundary of libseemps_gb300.so (declared in include/seemps_gb300.h).
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "kernels.cuh"
+
+namespace sm {
+
+template <typename T>
+int simplify_impl(Ctx&, cudaStream_t, int, const int*, int, const double*, const double*,
+                  const int*, const void* const*, const sm_strategy&, int, void* const*,
+                  const int64_t*, int*, sm_simplify_report*);
+template <typename T>
+int canonicalize_impl(Ctx&, cudaStream_t, int, const int*, int*, void* const*, const int64_t*,
+                      int, const sm_strategy&, double*);
+template <typename T>
+int scprod_impl(Ctx&, cudaStream_t, int, const int*, const int*, const void* const*, const int*,
+                const void* const*, double*);
+
+static thread_local std::string g_error;
+void set_error(const std::string& msg) { g_error = msg; }
+const char* last_error() { return g_error.c_str(); }
+
+Ctx::~Ctx() {
+  for (auto& kv : bufs)
+    if (kv.second.first) cudaFree(kv.second.first);
+  if (pinned) cudaFreeHost(pinned);
+}
+
+int Ctx::scratch(const std::string& name, size_t bytes, void** out) {
+  bytes = std::max<size_t>(bytes, 16);
+  auto it = bufs.find(name);
+  if (it != bufs.end() && it->second.second >= bytes) {
+    *out = it->second.first;
+    return SM_OK;
+  }
+  if (it != bufs.end() && it->second.first) {
+    cudaError_t e = cudaFree(it->second.first);  // synchronises the device
+    it->second = {nullptr, 0};
+    if (e != cudaSuccess) {
+      set_error(std::string("cudaFree: ") + cudaGetErrorString(e));
+      return SM_ERR_CUDA;
+    }
+  }
+  // round up to reduce regrowth
+  size_t alloc = bytes + bytes / 8;
+  alloc = (alloc + 255) & ~size_t(255);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, alloc);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaMalloc of " + std::to_string(alloc) + " bytes for '" + name + "' failed: " +
+              cudaGetErrorString(e));
+    return SM_ERR_NOMEM;
+  }
+  bufs[name] = {p, alloc};
+  *out = p;
+  return SM_OK;
+}
+
+static int check_strategy(const sm_strategy* st) {
+  if (!st) {
+    set_error("null strategy");
+    return SM_ERR_VALUE;
+  }
+  if (st->tolerance < 0 || st->tolerance >= 1.0) {
+    set_error("Invalid tolerance argument passed to Strategy");
+    return SM_ERR_STRATEGY;
+  }
+  if (st->max_bond_dimension <= 0) {
+    set_error("Invalid bond dimension in Strategy");
+    return SM_ERR_STRATEGY;
+  }
+  if (st->method < 0 || st->method > 3) {
+    set_error("Invalid method argument passed to Strategy");
+    return SM_ERR_STRATEGY;
+  }
+  if (st->simplify < 0 || st->simplify > 3) {
+    set_error("Invalid simplify argument passed to Strategy");
+    return SM_ERR_STRATEGY;
+  }
+  if (st->max_sweeps < 0) {
+    set_error("Negative or zero number of sweeps in Strategy");
+    return SM_ERR_STRATEGY;
+  }
+  return SM_OK;
+}
+
+static int check_dtype(int dtype) {
+  if (dtype != SM_FLOAT64 && dtype != SM_COMPLEX128) {
+    set_error("dtype must be SM_FLOAT64 or SM_COMPLEX128");
+    return SM_ERR_VALUE;
+  }
+  return SM_OK;
+}
+
+static Ctx* as_ctx(void* c) { return reinterpret_cast<Ctx*>(c); }
+static cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+#define SM_GUARD_CTX(c)                  \
+  if (!(c)) {                            \
+    ::sm::set_error("null context");     \
+    return SM_ERR_VALUE;                 \
+  }
+
+template <typename T>
+static int split2(Ctx* ctx, cudaStream_t st, const void* AA, int a, int d1, int d2, int b,
+                  const sm_strategy* s, int lmode, void* L, int rmode, void* R, int* D,
+                  double* err) {
+  SplitResult r;
+  SM_CHECK(svd_split<T>(*ctx, st, reinterpret_cast<const T*>(AA), a * d1, d2 * b, *s, lmode,
+                        reinterpret_cast<T*>(L), rmode, reinterpret_cast<T*>(R), nullptr, &r));
+  *D = r.D;
+  *err = std::sqrt(r.err2);
+  return SM_OK;
+}
+
+template <typename T>
+static int env_left(Ctx* ctx, cudaStream_t st, const void* B, int l, int j, int n, const void* A,
+                    int i, int k, const void* rho, void* out) {
+  T* tmp;
+  SM_CHECK(ctx->scratch("abi.env", (size_t)l * j * k, &tmp));
+  const T one = S<T>::one(), zero = S<T>::zero();
+  SM_CHECK(gemm<T>(st, SM_OP_N, SM_OP_N, l, j * k, i, one, (const T*)rho, i, (const T*)A, j * k,
+                   zero, tmp, j * k));
+  return gemm<T>(st, SM_OP_C, SM_OP_N, n, k, l * j, one, (const T*)B, n, tmp, k, zero, (T*)out, k);
+}
+
+template <typename T>
+static int env_right(Ctx* ctx, cudaStream_t st, const void* B, int l, int j, int n,
+                     const void* A, int i, int k, const void* rho, void* out) {
+  T* tmp;
+  SM_CHECK(ctx->scratch("abi.env", (size_t)i * j * n, &tmp));
+  const T one = S<T>::one(), zero = S<T>::zero();
+  SM_CHECK(gemm<T>(st, SM_OP_N, SM_OP_N, i * j, n, k, one, (const T*)A, k, (const T*)rho, n, zero,
+                   tmp, n));
+  return gemm<T>(st, SM_OP_N, SM_OP_C, i, l, j * n, one, tmp, j * n, (const T*)B, j * n, zero,
+                 (T*)out, l);
+}
+
+}  // namespace sm
+
+using namespace sm;
+
+extern "C" {
+
+int sm_abi_version(void) { return SM_ABI_VERSION; }
+
+const char* sm_last_error(void) { return sm::last_error(); }
+
+int sm_ctx_create(void** out, int device) {
+  if (!out) return SM_ERR_VALUE;
+  *out = nullptr;
+  SM_CUDA_CHECK(cudaSetDevice(device));
+  Ctx* c = new Ctx();
+  c->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaHostAlloc(&c->pinned, 64 * 1024, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    set_error(std::string("context creation: ") + cudaGetErrorString(e));
+    delete c;
+    return SM_ERR_CUDA;
+  }
+  *out = c;
+  return SM_OK;
+}
+
+int sm_ctx_destroy(void* ctx) {
+  if (!ctx) return SM_OK;
+  cudaDeviceSynchronize();
+  delete as_ctx(ctx);
+  return SM_OK;
+}
+
+int sm_truncate(void* ctx, const double* s_dev, int n, const sm_strategy* st, int* rank,
+                double* err2, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_strategy(st));
+  if (n < 1 || !s_dev || !rank || !err2) {
+    set_error("sm_truncate: need n >= 1 and non-null pointers");
+    return SM_ERR_VALUE;
+  }
+  return truncate_device(*as_ctx(ctx), as_stream(stream), s_dev, n, *st, rank, err2);
+}
+
+int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const void* A, int lda,
+            const void* B, int ldb, void* C, int ldc, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (opA < 0 || opA > 2 || opB < 0 || opB > 2) {
+    set_error("sm_gemm: invalid op flag");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return gemm<double>(as_stream(stream), opA, opB, M, N, K, 1.0, (const double*)A, lda,
+                        (const double*)B, ldb, 0.0, (double*)C, ldc);
+  return gemm<cplx>(as_stream(stream), opA, opB, M, N, K, cplx{1.0, 0.0}, (const cplx*)A, lda,
+                    (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc);
+}
+
+int sm_svd(void* ctx, int dtype, const void* A, int m, int n, void* U, double* s, void* Vt,
+           void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  sm_strategy st{};
+  st.method = SM_DO_NOT_TRUNCATE;
+  st.max_bond_dimension = 0x7fffffff;
+  SplitResult r;
+  if (dtype == SM_FLOAT64)
+    return svd_split<double>(*as_ctx(ctx), as_stream(stream), (const double*)A, m, n, st, OUT_U,
+                             (double*)U, OUT_VT, (double*)Vt, s, &r);
+  return svd_split<cplx>(*as_ctx(ctx), as_stream(stream), (const cplx*)A, m, n, st, OUT_U, (cplx*)U,
+                         OUT_VT, (cplx*)Vt, s, &r);
+}
+
+int sm_left_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int d2, int b,
+                       const sm_strategy* st, void* U, void* SV, int* D, double* err,
+                       void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_strategy(st));
+  if (dtype == SM_FLOAT64)
+    return split2<double>(as_ctx(ctx), as_stream(stream), AA, a, d1, d2, b, st, OUT_U, U, OUT_SVT,
+                          SV, D, err);
+  return split2<cplx>(as_ctx(ctx), as_stream(stream), AA, a, d1, d2, b, st, OUT_U, U, OUT_SVT, SV,
+                      D, err);
+}
+
+int sm_right_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int d2, int b,
+                        const sm_strategy* st, void* US, void* V, int* D, double* err,
+                        void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_strategy(st));
+  if (dtype == SM_FLOAT64)
+    return split2<double>(as_ctx(ctx), as_stream(stream), AA, a, d1, d2, b, st, OUT_US, US, OUT_VT,
+                          V, D, err);
+  return split2<cplx>(as_ctx(ctx), as_stream(stream), AA, a, d1, d2, b, st, OUT_US, US, OUT_VT, V,
+                      D, err);
+}
+
+int sm_update_left_environment(void* ctx, int dtype, const void* B, int l, int j, int n,
+                               const void* A, int i, int k, const void* rho, void* out,
+                               void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (l <= 0 || j <= 0 || n <= 0 || i <= 0 || k <= 0) {
+    set_error("Invalid arguments to _update_left_environment");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return env_left<double>(as_ctx(ctx), as_stream(stream), B, l, j, n, A, i, k, rho, out);
+  return env_left<cplx>(as_ctx(ctx), as_stream(stream), B, l, j, n, A, i, k, rho, out);
+}
+
+int sm_update_right_environment(void* ctx, int dtype, const void* B, int l, int j, int n,
+                                const void* A, int i, int k, const void* rho, void* out,
+                                void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (l <= 0 || j <= 0 || n <= 0 || i <= 0 || k <= 0) {
+    set_error("Invalid arguments to _update_right_environment");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return env_right<double>(as_ctx(ctx), as_stream(stream), B, l, j, n, A, i, k, rho, out);
+  return env_right<cplx>(as_ctx(ctx), as_stream(stream), B, l, j, n, A, i, k, rho, out);
+}
+
+int sm_mpo_multiply_tensor(void* ctx, int dtype, const void* O, int a, int i, int j, int b,
+                           const void* B, int c, int d, void* C, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (a <= 0 || i <= 0 || j <= 0 || b <= 0 || c <= 0 || d <= 0) {
+    set_error("Invalid arguments to _mpo_multiply_tensor");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return mpo_multiply_tensor<double>(as_stream(stream), (const double*)O, a, i, j, b,
+                                       (const double*)B, c, d, (double*)C);
+  return mpo_multiply_tensor<cplx>(as_stream(stream), (const cplx*)O, a, i, j, b, (const cplx*)B, c,
+                                   d, (cplx*)C);
+}
+
+int sm_scprod(void* ctx, int dtype, int L, const int* phys, const int* bra_bonds,
+              const void* const* bra, const int* ket_bonds, const void* const* ket, double* out,
+              void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (L < 1) {
+    set_error("Invalid arguments to scprod");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return scprod_impl<double>(*as_ctx(ctx), as_stream(stream), L, phys, bra_bonds, bra, ket_bonds,
+                               ket, out);
+  return scprod_impl<cplx>(*as_ctx(ctx), as_stream(stream), L, phys, bra_bonds, bra, ket_bonds, ket,
+                           out);
+}
+
+int sm_canonicalize(void* ctx, int dtype, int L, const int* phys, int* bonds, void* const* sites,
+                    const int64_t* cap, int center, const sm_strategy* st, double* err,
+                    void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_strategy(st));
+  if (L < 1 || center < 0 || center >= L) {
+    set_error("canonicalize: center out of range");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return canonicalize_impl<double>(*as_ctx(ctx), as_stream(stream), L, phys, bonds, sites, cap,
+                                     center, *st, err);
+  return canonicalize_impl<cplx>(*as_ctx(ctx), as_stream(stream), L, phys, bonds, sites, cap,
+                                 center, *st, err);
+}
+
+int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms, const double* weights,
+                const int* ket_bonds, const void* const* ket_sites, const double* term_errors,
+                const sm_strategy* st, int direction, void* const* out_sites,
+                const int64_t* out_cap, int* out_bonds, sm_simplify_report* rep, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_strategy(st));
+  if (L < 1 || nterms < 1 || !rep || !weights || !ket_bonds || !ket_sites) {
+    set_error("simplify: need L >= 1, nterms >= 1 and non-null arguments");
+    return SM_ERR_VALUE;
+  }
+  for (int t = 0; t < nterms; ++t) {
+    const int* kb = ket_bonds + (size_t)t * (L + 1);
+    for (int i = 0; i < L; ++i)
+      if (kb[i] <= 0 || phys[i] <= 0) {
+        set_error("simplify: non-positive dimension");
+        return SM_ERR_VALUE;
+      }
+    if (kb[0] != 1 || kb[L] != 1) {
+      set_error("simplify: open boundary bonds must be 1");
+      return SM_ERR_VALUE;
+    }
+  }
+  if (dtype == SM_FLOAT64)
+    return simplify_impl<double>(*as_ctx(ctx), as_stream(stream), L, phys, nterms, weights,
+                                 term_errors, ket_bonds, ket_sites, *st, direction, out_sites,
+                                 out_cap, out_bonds, rep);
+  return simplify_impl<cplx>(*as_ctx(ctx), as_stream(stream), L, phys, nterms, weights,
+                             term_errors, ket_bonds, ket_sites, *st, direction, out_sites, out_cap,
+                             out_bonds, rep);
+}
+
+int sm_simplify_bond_caps(int L, const int* phys, int nterms, const int* ket_bonds,
+                          const sm_strategy* st, int* cap_bonds) {
+  SM_CHECK(check_strategy(st));
+  if (L < 1 || nterms < 1) {
+    set_error("bond caps: need L >= 1 and nterms >= 1");
+    return SM_ERR_VALUE;
+  }
+  (void)phys;
+  for (int i = 0; i <= L; ++i) {
+    long long K = 0;
+    for (int t = 0; t < nterms; ++t) K += ket_bonds[(size_t)t * (L + 1) + i];
+    if (nterms > 1 && (i == 0 || i == L)) K = 1;
+    long long c = std::min<long long>(K, st->max_bond_dimension);
+    if (i == 0 || i == L) c = K;
+    cap_bonds[i] = (int)std::max<long long>(1, c);
+  }
+  return SM_OK;
+}
+
+int sm_trace_enable(void* ctx, int on) {
+  SM_GUARD_CTX(ctx);
+  Ctx* c = as_ctx(ctx);
+  c->trace = on != 0;
+  c->tr_rank.clear();
+  c->tr_len.clear();
+  c->tr_err2.clear();
+  c->tr_s.clear();
+  return SM_OK;
+}
+
+int sm_trace_read(void* ctx, int* count, int64_t* total_s, int* ranks, int* lens, double* err2,
+                  double* svals) {
+  SM_GUARD_CTX(ctx);
+  Ctx* c = as_ctx(ctx);
+  if (count) *count = (int)c->tr_rank.size();
+  if (total_s) *total_s = (int64_t)c->tr_s.size();
+  if (ranks) std::copy(c->tr_rank.begin(), c->tr_rank.end(), ranks);
+  if (lens) std::copy(c->tr_len.begin(), c->tr_len.end(), lens);
+  if (err2) std::copy(c->tr_err2.begin(), c->tr_err2.end(), err2);
+  if (svals) std::copy(c->tr_s.begin(), c->tr_s.end(), svals);
+  return SM_OK;
+}
+
+int sm_probe_fp64(void* ctx, int blocks, int threads, int iters, double* ms, double* flops,
+                  void* stream) {
+  SM_GUARD_CTX(ctx);
+  return probe_fp64(as_stream(stream), blocks, threads, iters, ms, flops);
+}
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// FP64 / complex128 GEMM for the contractions of the sweep (row-major).
+//
+//   C[M,N] = alpha * op(A)[M,K] * op(B)[K,N] + beta * C
+//
+// op = N (as stored), T (transpose) or C (conjugate transpose), the three
+// GemmOrder flags of the reference (cython/gemm.pxi:17-20, :21-122).  GB300
+// runs FP64 on the CUDA cores only, so this is a shared-memory tiled SIMT
+// kernel: 64x64 output tile per CTA, 16-deep K slices, 256 threads holding a
+// 4x4 register tile each; the FP64 pipe is the bound, not HBM (operands are
+// re-read from L2 at most M/64 + N/64 times).
+#include "kernels.cuh"
+
+namespace sm {
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+template <typename T>
+__device__ __forceinline__ T load_op(const T* p, int op) {
+  T v = __ldg(p);
+  return op == SM_OP_C ? S<T>::conj(v) : v;
+}
+template <>
+__device__ __forceinline__ cplx load_op<cplx>(const cplx* p, int op) {
+  const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+  return op == SM_OP_C ? cplx{v.x, -v.y} : cplx{v.x, v.y};
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int K, T alpha,
+                                             const T* __restrict__ A, int lda,
+                                             const T* __restrict__ B, int ldb, T beta,
+                                             T* __restrict__ C, int ldc) {
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = S<T>::zero();
+
+  for (int k0 = 0; k0 < K; k0 += BK) {
+#pragma unroll
+    for (int e = 0; e < (BM * BK) / NT; ++e) {
+      const int idx = tid + e * NT;
+      int mm, kk;
+      if (opA == SM_OP_N) { mm = idx / BK; kk = idx % BK; }
+      else                { kk = idx / BM; mm = idx % BM; }
+      const int gm = m0 + mm, gk = k0 + kk;
+      T v = S<T>::zero();
+      if (gm < M && gk < K)
+        v = opA == SM_OP_N ? load_op(A + (size_t)gm * lda + gk, opA)
+                           : load_op(A + (size_t)gk * lda + gm, opA);
+      As[kk][mm] = v;
+    }
+#pragma unroll
+    for (int e = 0; e < (BN * BK) / NT; ++e) {
+      const int idx = tid + e * NT;
+      int nn, kk;
+      if (opB == SM_OP_N) { kk = idx / BN; nn = idx % BN; }
+      else                { nn = idx / BK; kk = idx % BK; }
+      const int gn = n0 + nn, gk = k0 + kk;
+      T v = S<T>::zero();
+      if (gn < N && gk < K)
+        v = opB == SM_OP_N ? load_op(B + (size_t)gk * ldb + gn, opB)
+                           : load_op(B + (size_t)gn * ldb + gk, opB);
+      Bs[kk][nn] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = S<T>::fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  const bool use_beta = S<T>::abs2(beta) != 0.0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + tx + 16 * j;
+      if (gn >= N) continue;
+      T* c = C + (size_t)gm * ldc + gn;
+      T v = alpha * acc[i][j];
+      if (use_beta) v = S<T>::fma(beta, *c, v);
+      *c = v;
+    }
+  }
+}
+
+}  // namespace
+
+template <typename T>
+int gemm(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda,
+         const T* B, int ldb, T beta, T* C, int ldc) {
+  if (M < 0 || N < 0 || K < 0) {
+    set_error("gemm: negative size");
+    return SM_ERR_VALUE;
+  }
+  if (M == 0 || N == 0) return SM_OK;
+  if (K == 0) {
+    // C = beta C  (or zero)
+    return scale_matrix<T>(st, M, N, beta, C, ldc);
+  }
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+  if (grid.y > 65535) {
+    set_error("gemm: M too large");
+    return SM_ERR_VALUE;
+  }
+  k_gemm<T><<<grid, NT, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
+}
+
+template int gemm<double>(cudaStream_t, int, int, int, int, int, double, const double*, int,
+                          const double*, int, double, double*, int);
+template int gemm<cplx>(cudaStream_t, int, int, int, int, int, cplx, const cplx*, int,
+                        const cplx*, int, cplx, cplx*, int);
+
+}  // namespace sm

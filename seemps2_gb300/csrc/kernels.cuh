@@ -1,0 +1,92 @@
+// Internal (C++) interface between the kernels, the sweep driver and the C ABI.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sm {
+
+// ---------------------------------------------------------------------------
+// Context: scratch device buffers (grown on demand, reused across calls) and a
+// small pinned host block for reading back ranks / scalars.
+// ---------------------------------------------------------------------------
+struct Ctx {
+  int device = 0;
+  int num_sms = 0;
+  void* pinned = nullptr;  // 64 KB of pinned host memory
+  std::map<std::string, std::pair<void*, size_t>> bufs;
+  std::map<const void*, int> coop_blocks;  // per-kernel co-resident CTA limit
+  // split trace (sm_trace_*): one record per SVD split, singular values included
+  bool trace = false;
+  std::vector<int> tr_rank, tr_len;
+  std::vector<double> tr_err2, tr_s;
+  ~Ctx();
+  // Returns a device buffer of at least `bytes` bytes for `name`.  A buffer
+  // only grows; growing it synchronises the device (cudaFree).
+  int scratch(const std::string& name, size_t bytes, void** out);
+  template <typename P>
+  int scratch(const std::string& name, size_t count, P** out) {
+    return scratch(name, count * sizeof(P), reinterpret_cast<void**>(out));
+  }
+};
+
+// Kept size and squared discarded weight of a split.
+struct SplitResult {
+  int D;
+  int status;
+  double err2;
+  int sweeps;
+  int pad;
+};
+
+// Output forms of the two factors of a split A = U diag(s) Vt.
+enum { OUT_NONE = 0, OUT_U = 1, OUT_US = 2 };
+enum { OUT_VT = 1, OUT_SVT = 2 };
+
+// --- gemm.cu ---------------------------------------------------------------
+template <typename T>
+int gemm(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda,
+         const T* B, int ldb, T beta, T* C, int ldc);
+
+// --- mps_ops.cu ------------------------------------------------------------
+template <typename T>
+int scale_matrix(cudaStream_t st, int M, int N, T beta, T* C, int ldc);
+template <typename T>
+int scale_vector(cudaStream_t st, size_t n, double factor, T* x);
+template <typename T>
+int fill_zero(cudaStream_t st, size_t n, T* x);
+template <typename T>
+int mpo_multiply_tensor(cudaStream_t st, const T* O, int a, int i, int j, int b, const T* B,
+                        int c, int d, T* C);
+// out[0] (+ out[1] for complex) = sum conj(x) y, deterministic two-pass reduction
+template <typename T>
+int vdot(Ctx& ctx, cudaStream_t st, size_t n, const T* x, const T* y, double* out_dev);
+template <typename T>
+int transpose(cudaStream_t st, int m, int n, const T* A, int lda, T* B, int ldb);
+template <typename T>
+int set_identity(cudaStream_t st, int k, T* X, int ldx);
+// Copy `n` elements of the mixed-dtype buffers used by the joined MPSSum guess.
+template <typename T>
+int copy_block3(cudaStream_t st, const T* src, int a, int d, int b, T* dst, int A, int B,
+                int off_a, int off_b, T w);
+int probe_fp64(cudaStream_t st, int blocks, int threads, int iters, double* ms, double* flops);
+
+// --- svd.cu ----------------------------------------------------------------
+// Exact reference truncation rule on device values s_dev[0..n) (descending).
+int truncate_device(Ctx& ctx, cudaStream_t st, const double* s_dev, int n,
+                    const sm_strategy& strat, int* rank, double* err2);
+
+// SVD of A (m x n, row-major, leading dim n) followed by truncation with
+// `strat`.  Writes the left factor (m x D, mode OUT_U / OUT_US) into `left`
+// and the right factor (D x n, mode OUT_VT / OUT_SVT) into `right`; optional
+// `s_out` receives all min(m,n) singular values (descending).  The kept size
+// D and err^2 are returned on the host (one stream synchronisation).
+template <typename T>
+int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
+              int left_mode, T* left, int right_mode, T* right, double* s_out,
+              SplitResult* res);
+
+}  // namespace sm

@@ -1,0 +1,148 @@
+"""MPO and MPOList with ``apply`` / ``@`` on the GPU (operators/mpo.py:48-753)."""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .core import DEFAULT_STRATEGY, Strategy, _mpo_multiply_tensor, as_device
+from .state import MPS, MPSSum, TensorArray, simplify
+
+
+class MPO(TensorArray):
+    """Matrix product operator ``O[a, i, j, b]`` (operators/mpo.py:48-75)."""
+
+    __array_priority__ = 10000
+
+    def __init__(self, data, strategy: Strategy = DEFAULT_STRATEGY):
+        data = list(data)
+        cplx = any((t.is_complex() if hasattr(t, "is_complex") else np.iscomplexobj(t)) for t in data)
+        super().__init__([as_device(t, cplx) for t in data])
+        self.strategy = strategy
+
+    def copy(self) -> "MPO":
+        return MPO(self._data, self.strategy)
+
+    def physical_dimensions(self) -> list[int]:
+        return [int(A.shape[2]) for A in self._data]
+
+    def bond_dimensions(self) -> list[int]:
+        return [int(A.shape[-1]) for A in self._data][:-1]
+
+    def max_bond_dimension(self) -> int:
+        return max(int(A.shape[0]) for A in self._data)
+
+    @property
+    def T(self) -> "MPO":
+        return MPO([A.permute(0, 2, 1, 3).contiguous() for A in self._data], self.strategy)
+
+    def conj(self) -> "MPO":
+        return MPO([A.conj().resolve_conj() for A in self._data], self.strategy)
+
+    def set_strategy(self, strategy: Strategy) -> "MPO":
+        return MPO(self._data, strategy)
+
+    def __mul__(self, n):
+        if isinstance(n, (int, float, complex)):
+            absn = abs(n)
+            if absn:
+                phase = n / absn
+                factor = np.exp(np.log(absn) / self.size)
+            else:
+                phase, factor = 0.0, 0.0
+            return MPO([(factor if i > 0 else factor * phase) * A for i, A in enumerate(self._data)],
+                       self.strategy)
+        raise TypeError(f"Cannot multiply MPO by {type(n)}")
+
+    __rmul__ = __mul__
+
+    def to_matrix(self):
+        """Dense matrix (small systems only)."""
+        import torch
+
+        out = torch.ones((1, 1, 1), dtype=self._data[0].dtype, device=self._data[0].device)
+        Di = Dj = 1
+        for A in self._data:
+            _, i, j, b = A.shape
+            Di *= i
+            Dj *= j
+            out = torch.tensordot(out, A, dims=1).permute(0, 2, 1, 3, 4).reshape(Di, Dj, b)
+        return out[:, :, 0]
+
+    def apply(self, state, strategy: Strategy | None = None, simplify: bool | None = None):
+        """``self @ state`` followed by ``simplify`` when the strategy asks for it
+        (operators/mpo.py:229-281)."""
+        if strategy is None:
+            strategy = self.strategy
+        if strategy is None:
+            raise RuntimeError("MPO has no truncation strategy")
+        if simplify is None:
+            simplify = strategy.get_simplify_flag()
+        if isinstance(state, MPSSum):
+            if self.size != state.size:
+                raise ValueError("MPO and state must have the same size")
+            out = None
+            for i, (w, mps) in enumerate(zip(state.weights, state.states)):
+                Ostate = w * MPS([_mpo_multiply_tensor(A, B) for A, B in zip(self._data, mps._data)],
+                                 error=mps.error())
+                out = Ostate if i == 0 else out + Ostate
+            state = out
+        elif isinstance(state, MPS):
+            if self.size != state.size:
+                raise ValueError("MPO and state must have the same size")
+            state = MPS([_mpo_multiply_tensor(A, B) for A, B in zip(self._data, state._data)],
+                        error=state.error())
+        else:
+            raise TypeError(f"Cannot multiply MPO with {state}")
+        if simplify:
+            state = _simplify(state, strategy=strategy)
+        return state
+
+    def __matmul__(self, b):
+        if isinstance(b, (MPS, MPSSum)):
+            return self.apply(b)
+        if isinstance(b, MPO):
+            return MPOList([b, self])
+        if isinstance(b, MPOList):
+            return MPOList(b.mpos + [self], b.strategy)
+        raise TypeError(f"Cannot multiply MPO with {b}")
+
+    def __rmatmul__(self, b):
+        if isinstance(b, (MPS, MPSSum)):
+            return self.T.apply(b)
+        raise TypeError(f"Cannot multiply {b} with MPO")
+
+
+_simplify = simplify
+
+
+class MPOList:
+    """Sequence of MPOs applied right-to-left order of the list (operators/mpo.py:430-621)."""
+
+    def __init__(self, mpos, strategy: Strategy = DEFAULT_STRATEGY):
+        self.mpos = list(mpos)
+        self.size = self.mpos[0].size
+        self.strategy = strategy
+
+    def copy(self) -> "MPOList":
+        return MPOList(self.mpos, self.strategy)
+
+    def apply(self, state, strategy: Strategy | None = None, simplify: bool | None = None):
+        """Each MPO applied with its own strategy, then one final simplify (:585-621)."""
+        if strategy is None:
+            strategy = self.strategy
+        if simplify is None:
+            simplify = strategy.get_simplify_flag()
+        for mpo in self.mpos:
+            state = mpo.apply(state)
+        if simplify:
+            state = _simplify(state, strategy=strategy)
+        return state
+
+    def __matmul__(self, b):
+        if isinstance(b, (MPS, MPSSum)):
+            return self.apply(b)
+        if isinstance(b, MPO):
+            return MPOList([b] + self.mpos, self.strategy)
+        if isinstance(b, MPOList):
+            return MPOList(b.mpos + self.mpos, self.strategy)
+        raise TypeError(f"Cannot multiply MPOList with {b}")

@@ -1,0 +1,119 @@
+"""End-to-end parity of MPO.apply / simplify on the GPU against the oracle and
+the reference's golden runs: identical kept ranks at every split, singular
+values within 1e-10 * s_max, state fidelity error below 1e-12."""
+
+import numpy as np
+import pytest
+
+from oracle import seemps_oracle as so
+from tests.golden_cases import CASE_NAMES, load_case, run_oracle, strategy_for
+from tests.gpu_util import mps_np, sv_close
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import seemps2_gb300 as sg  # noqa: E402
+from seemps2_gb300 import _lib  # noqa: E402
+
+
+def run_gpu(p, mps, mpo):
+    st = strategy_for(p, sg)
+    psi = sg.MPS(mps)
+    with _lib.SplitTrace() as tr:
+        if p["kind"] in ("mpo_apply", "laplacian"):
+            out = sg.MPO(mpo, st).apply(psi, strategy=st)
+        elif p["kind"] == "euler":
+            Lx = sg.MPO(mpo, st).apply(psi, simplify=False)
+            out = sg.simplify(sg.MPSSum([1.0, p["dt"]], [psi, Lx]), strategy=st)
+        else:
+            out = sg.simplify(psi, strategy=st)
+    return out, tr
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_parity_with_reference_run(name):
+    p, mps, mpo, g, same = load_case(name)
+    out, tr = run_gpu(p, mps, mpo)
+    rec = so.Recorder()
+    res, _ = run_oracle(p, mps, mpo, rec)
+    # identical truncation decisions at every split, in the same order
+    assert tr.ranks == [sp.rank for sp in rec.splits]
+    for s_gpu, sp in zip(tr.s, rec.splits):
+        sv_close(s_gpu, sp.s, 1e-10)
+    if same:  # the fixture was made from these very inputs: compare with the reference too
+        assert tr.ranks == g["split_rank"].tolist()
+        assert out.bond_dimensions() == g["bonds"].tolist()
+        assert out.center == int(g["center"])
+    assert out.bond_dimensions() == [A.shape[0] for A in res.tensors] + [1]
+    fe = so.fidelity_error(mps_np(out), res.tensors)
+    assert fe < 1e-12, fe
+    e1, e2 = out.error() ** 2, res.error ** 2
+    assert abs(e1 - e2) <= 1e-13 + 1e-8 * e2
+
+
+@pytest.mark.parametrize("method", [0, 1, 2, 3])
+def test_canonical_form_matches_oracle(method):
+    rng = np.random.default_rng(5)
+    mps = so.random_mps(2, 9, 12, rng, complex_=True)
+    st = sg.Strategy(method=method, tolerance=1e-6 if method else 1e-3, max_bond_dimension=9)
+    ost = so.Strategy(method=method, tolerance=1e-6 if method else 1e-3, max_bond_dimension=9)
+    for center in (0, 4, 8, -1):
+        c = sg.CanonicalMPS(mps, center=center, strategy=st)
+        ref, rc, err = so.canonical_mps(mps, center, ost)
+        assert c.center == rc
+        assert c.bond_dimensions() == [A.shape[0] for A in ref] + [1]
+        assert so.fidelity_error(mps_np(c), ref) < 1e-12
+        assert abs(c.error() - err) <= 1e-9 * max(1, err)
+        # isometries left and right of the centre (test_canonical.py:18-146)
+        for i, A in enumerate(mps_np(c)):
+            a, d, b = A.shape
+            if i < rc:
+                M = A.reshape(a * d, b)
+                assert np.allclose(M.conj().T @ M, np.eye(b), atol=1e-11)
+            elif i > rc:
+                M = A.reshape(a, d * b)
+                assert np.allclose(M @ M.conj().T, np.eye(a), atol=1e-11)
+
+
+def test_recenter_and_scprod():
+    rng = np.random.default_rng(9)
+    mps = so.random_mps(2, 8, 10, rng)
+    c = sg.CanonicalMPS(mps, center=0)
+    c.recenter(5)
+    assert c.center == 5
+    assert so.fidelity_error(mps_np(c), mps) < 1e-12
+    assert abs(sg.scprod(sg.MPS(mps), sg.MPS(mps)) - so.scprod(mps, mps)) <= 1e-10 * abs(so.scprod(mps, mps))
+
+
+def test_simplification_methods_and_no_truncation():
+    """test_simplify.py:6-54: exact without truncation; CANONICAL_FORM == VARIATIONAL."""
+    rng = np.random.default_rng(11)
+    for n in range(3, 9):
+        mps = so.random_mps(2, n, int(2 ** (n / 2)), rng, truncate_=False)
+        mps = so.scale(mps, 1 / np.sqrt(so.norm_squared(mps)))
+        psi = sg.MPS(mps)
+        st = sg.DEFAULT_STRATEGY.replace(method=sg.Truncation.DO_NOT_TRUNCATE)
+        phi = sg.simplify(psi, strategy=st)
+        assert so.fidelity_error(mps_np(phi), mps) < 1e-12
+        phi0 = sg.simplify(psi, strategy=sg.DEFAULT_STRATEGY.replace(simplify=sg.Simplification.CANONICAL_FORM))
+        phi1 = sg.simplify(psi, strategy=sg.DEFAULT_STRATEGY.replace(simplify=sg.Simplification.VARIATIONAL))
+        assert so.fidelity_error(mps_np(phi0), mps_np(phi1)) < 1e-12
+
+
+def test_max_bond_dimension_respected():
+    rng = np.random.default_rng(12)
+    mps = so.random_mps(2, 14, 128, rng)
+    psi = sg.MPS(mps)
+    for D in (2, 5, 14):
+        phi = sg.simplify(psi, strategy=sg.DEFAULT_STRATEGY.replace(max_bond_dimension=D))
+        assert max(phi.bond_dimensions()) <= D
+
+
+def test_zero_state():
+    mps = [np.zeros((1, 2, 2)), np.zeros((2, 2, 1))]
+    out = sg.simplify(sg.MPS(mps))
+    assert out.bond_dimensions() == [1, 1, 1]
+    assert out.norm_squared() == 0.0
