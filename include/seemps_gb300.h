@@ -174,6 +174,25 @@ int sm_trace_enable(void* ctx, int on);
 int sm_trace_read(void* ctx, int* count, int64_t* total_s, int* ranks, int* lens,
                   double* err2, double* svals);
 
+/* Counters of this context.  Launch counts are always kept; per-kernel device
+ * times (CUDA events around each Jacobi SVD launch and each GEMM) are only
+ * recorded while timing is enabled.  Algorithmic flops follow the usual
+ * convention: 2MNK per real GEMM (x4 complex), 4mn^2 + 8n^3 per m x n SVD
+ * (m >= n, x4 complex). */
+typedef struct sm_stats {
+  int64_t launches;        /* kernels launched by this library */
+  int64_t jacobi_launches;
+  int64_t jacobi_sweeps;   /* Jacobi sweeps summed over launches */
+  int64_t gemm_launches;
+  int64_t splits;          /* SVD splits */
+  double jacobi_ms;        /* event-timed device time of the Jacobi kernels */
+  double jacobi_flops;     /* algorithmic SVD flops of those launches */
+  double gemm_ms;          /* event-timed device time of the GEMMs */
+  double gemm_flops;
+} sm_stats;
+int sm_stats_reset(void* ctx, int timing);
+int sm_stats_read(void* ctx, sm_stats* out);
+
 /* Device FP64 throughput probe: runs `iters` dependent FMA chains per thread
  * over the given grid and reports elapsed milliseconds (CUDA events). */
 int sm_probe_fp64(void* ctx, int blocks, int threads, int iters, double* ms,

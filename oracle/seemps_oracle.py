@@ -27,6 +27,8 @@ from math import sqrt
 
 import numpy as np
 import scipy.linalg
+import scipy.linalg.blas
+import scipy.linalg.lapack
 
 # --------------------------------------------------------------------------
 # Strategy (reference cython/truncation.pxi:1-220, mirror _python_core.py:60-183)
@@ -161,21 +163,43 @@ def truncate(s: np.ndarray, strategy: Strategy) -> tuple[int, float]:
 
 
 def svd(A: np.ndarray):
-    """Economy SVD through LAPACK gesdd (reference svd.pxi:35-83)."""
+    """Economy SVD through LAPACK ?gesdd called directly, as the reference's
+    Cython core does (svd.pxi:35-83, gesdd being its default driver :23)."""
     if A.dtype == np.complex64:
         A = A.astype(np.complex128)
     elif A.dtype not in (np.float64, np.complex128):
         A = A.astype(np.float64)
-    return scipy.linalg.svd(
-        A, full_matrices=False, lapack_driver="gesdd", check_finite=False
-    )
+    f = scipy.linalg.lapack.zgesdd if np.iscomplexobj(A) else scipy.linalg.lapack.dgesdd
+    U, s, Vh, info = f(A, compute_uv=1, full_matrices=0)
+    if info > 0:
+        raise np.linalg.LinAlgError("SVD did not converge")
+    if info < 0:
+        raise RuntimeError(f"Wrong argument {-info} to LAPACK SVD.")
+    return U, s, Vh
+
+
+def gemm(A: np.ndarray, B: np.ndarray, opA: str = "N", opB: str = "N") -> np.ndarray:
+    """op(A) @ op(B) through SciPy's BLAS ?gemm, the library the reference's
+    _gemm calls (gemm.pxi:21-122).  Using one BLAS for GEMM and LAPACK keeps a
+    single OpenBLAS thread pool busy, as in the reference's process."""
+    cplx = np.iscomplexobj(A) or np.iscomplexobj(B)
+    dt = np.complex128 if cplx else np.float64
+    A = np.asarray(A, dtype=dt)
+    B = np.asarray(B, dtype=dt)
+    f = scipy.linalg.blas.zgemm if cplx else scipy.linalg.blas.dgemm
+    code = {"N": 0, "T": 1, "C": 2}
+    # row-major C = op(A) op(B)  <=>  column-major C^T = op(B)^T op(A)^T
+    Ct = f(1.0, B.T if B.flags.c_contiguous else np.asfortranarray(B.T),
+           A.T if A.flags.c_contiguous else np.asfortranarray(A.T),
+           trans_a=code[opB], trans_b=code[opA])
+    return Ct.T
 
 
 def contract_last_and_first(A: np.ndarray, B: np.ndarray) -> np.ndarray:
     """Contract the last index of A with the first of B (contractions.pxi:6-38)."""
-    Am = A.reshape(-1, A.shape[-1])
-    Bm = B.reshape(B.shape[0], -1)
-    return (Am @ Bm).reshape(A.shape[:-1] + B.shape[1:])
+    Am = np.ascontiguousarray(A.reshape(-1, A.shape[-1]))
+    Bm = np.ascontiguousarray(B.reshape(B.shape[0], -1))
+    return gemm(Am, Bm).reshape(A.shape[:-1] + B.shape[1:])
 
 
 def mpo_multiply_tensor(O: np.ndarray, B: np.ndarray) -> np.ndarray:
@@ -191,16 +215,16 @@ def update_left_environment(B: np.ndarray, A: np.ndarray, rho: np.ndarray):
     """rho'[n,k] = sum conj(B[l,j,n]) rho[l,i] A[i,j,k] (environments.pxi:10-37)."""
     l, j, n = B.shape
     i, j2, k = A.shape
-    tmp = (rho @ A.reshape(i, j * k)).reshape(l * j, k)
-    return B.reshape(l * j, n).conj().T @ tmp
+    tmp = np.ascontiguousarray(gemm(np.ascontiguousarray(rho), np.ascontiguousarray(A).reshape(i, j * k)))
+    return np.ascontiguousarray(gemm(np.ascontiguousarray(B).reshape(l * j, n), tmp.reshape(l * j, k), "C", "N"))
 
 
 def update_right_environment(B: np.ndarray, A: np.ndarray, rho: np.ndarray):
     """rho'[i,l] = sum A[i,j,k] rho[k,n] conj(B[l,j,n]) (environments.pxi:39-67)."""
     i, j, k = A.shape
     l, j2, n = B.shape
-    tmp = (A.reshape(i * j, k) @ rho).reshape(i, j * n)
-    return tmp @ B.reshape(l, j * n).conj().T
+    tmp = np.ascontiguousarray(gemm(np.ascontiguousarray(A).reshape(i * j, k), np.ascontiguousarray(rho)))
+    return np.ascontiguousarray(gemm(tmp.reshape(i, j * n), np.ascontiguousarray(B).reshape(l, j * n), "N", "C"))
 
 
 def scprod(bra: list, ket: list):
@@ -364,7 +388,7 @@ class AntilinearForm:
             j = self.center
             i = j - 1
         LA = contract_last_and_first(self.L[i], self.ket[i])
-        BR = np.matmul(self.ket[j], self.R[j])
+        BR = contract_last_and_first(self.ket[j], self.R[j])
         return contract_last_and_first(LA, BR)
 
     def update_right(self):

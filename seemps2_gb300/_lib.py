@@ -49,6 +49,20 @@ class sm_simplify_report(C.Structure):
     ]
 
 
+class sm_stats(C.Structure):
+    _fields_ = [
+        ("launches", C.c_int64),
+        ("jacobi_launches", C.c_int64),
+        ("jacobi_sweeps", C.c_int64),
+        ("gemm_launches", C.c_int64),
+        ("splits", C.c_int64),
+        ("jacobi_ms", C.c_double),
+        ("jacobi_flops", C.c_double),
+        ("gemm_ms", C.c_double),
+        ("gemm_flops", C.c_double),
+    ]
+
+
 vp = C.c_void_p
 ip = C.POINTER(C.c_int)
 dp = C.POINTER(C.c_double)
@@ -83,6 +97,8 @@ SIGNATURES = {
     "sm_simplify_bond_caps": (C.c_int, [C.c_int, ip, C.c_int, ip, stp, ip]),
     "sm_trace_enable": (C.c_int, [vp, C.c_int]),
     "sm_trace_read": (C.c_int, [vp, ip, i64p, ip, ip, dp, dp]),
+    "sm_stats_reset": (C.c_int, [vp, C.c_int]),
+    "sm_stats_read": (C.c_int, [vp, C.POINTER(sm_stats)]),
     "sm_probe_fp64": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, vp]),
 }
 
@@ -207,3 +223,13 @@ class SplitTrace:
         offs = np.concatenate([[0], np.cumsum([lens[k] for k in range(n.value)])]).astype(int)
         self.s = [allv[offs[k]:offs[k + 1]] for k in range(n.value)]
         return False
+
+
+def stats_reset(timing: bool = False, device: int = 0):
+    check(load().sm_stats_reset(context(device), int(timing)))
+
+
+def stats_read(device: int = 0) -> dict:
+    st = sm_stats()
+    check(load().sm_stats_read(context(device), C.byref(st)))
+    return {name: getattr(st, name) for name, _ in sm_stats._fields_}

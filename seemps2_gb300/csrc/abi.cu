@@ -1,5 +1,6 @@
 // extern "C" boundary of libseemps_gb300.so (declared in include/seemps_gb300.h).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <string>
 
@@ -19,10 +20,15 @@ int scprod_impl(Ctx&, cudaStream_t, int, const int*, const int*, const void* con
                 const void* const*, double*);
 
 static thread_local std::string g_error;
+static std::atomic<long long> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 void set_error(const std::string& msg) { g_error = msg; }
 const char* last_error() { return g_error.c_str(); }
 
 Ctx::~Ctx() {
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
   for (auto& kv : bufs)
     if (kv.second.first) cudaFree(kv.second.first);
   if (pinned) cudaFreeHost(pinned);
@@ -122,9 +128,10 @@ static int env_left(Ctx* ctx, cudaStream_t st, const void* B, int l, int j, int 
   T* tmp;
   SM_CHECK(ctx->scratch("abi.env", (size_t)l * j * k, &tmp));
   const T one = S<T>::one(), zero = S<T>::zero();
-  SM_CHECK(gemm<T>(st, SM_OP_N, SM_OP_N, l, j * k, i, one, (const T*)rho, i, (const T*)A, j * k,
-                   zero, tmp, j * k));
-  return gemm<T>(st, SM_OP_C, SM_OP_N, n, k, l * j, one, (const T*)B, n, tmp, k, zero, (T*)out, k);
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, l, j * k, i, one, (const T*)rho, i, (const T*)A,
+                       j * k, zero, tmp, j * k));
+  return gemm_ctx<T>(*ctx, st, SM_OP_C, SM_OP_N, n, k, l * j, one, (const T*)B, n, tmp, k, zero,
+                     (T*)out, k);
 }
 
 template <typename T>
@@ -133,10 +140,10 @@ static int env_right(Ctx* ctx, cudaStream_t st, const void* B, int l, int j, int
   T* tmp;
   SM_CHECK(ctx->scratch("abi.env", (size_t)i * j * n, &tmp));
   const T one = S<T>::one(), zero = S<T>::zero();
-  SM_CHECK(gemm<T>(st, SM_OP_N, SM_OP_N, i * j, n, k, one, (const T*)A, k, (const T*)rho, n, zero,
-                   tmp, n));
-  return gemm<T>(st, SM_OP_N, SM_OP_C, i, l, j * n, one, tmp, j * n, (const T*)B, j * n, zero,
-                 (T*)out, l);
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, i * j, n, k, one, (const T*)A, k, (const T*)rho,
+                       n, zero, tmp, n));
+  return gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_C, i, l, j * n, one, tmp, j * n, (const T*)B, j * n,
+                     zero, (T*)out, l);
 }
 
 }  // namespace sm
@@ -157,6 +164,8 @@ int sm_ctx_create(void** out, int device) {
   c->device = device;
   cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaHostAlloc(&c->pinned, 64 * 1024, cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e != cudaSuccess) {
     set_error(std::string("context creation: ") + cudaGetErrorString(e));
     delete c;
@@ -388,6 +397,23 @@ int sm_trace_read(void* ctx, int* count, int64_t* total_s, int* ranks, int* lens
   if (lens) std::copy(c->tr_len.begin(), c->tr_len.end(), lens);
   if (err2) std::copy(c->tr_err2.begin(), c->tr_err2.end(), err2);
   if (svals) std::copy(c->tr_s.begin(), c->tr_s.end(), svals);
+  return SM_OK;
+}
+
+int sm_stats_reset(void* ctx, int timing) {
+  SM_GUARD_CTX(ctx);
+  Ctx* c = as_ctx(ctx);
+  c->stats = sm_stats{};
+  c->stats.launches = -launches_total();  // read back as a difference
+  c->timing = timing != 0;
+  return SM_OK;
+}
+
+int sm_stats_read(void* ctx, sm_stats* out) {
+  SM_GUARD_CTX(ctx);
+  if (!out) return SM_ERR_VALUE;
+  *out = as_ctx(ctx)->stats;
+  out->launches += launches_total();
   return SM_OK;
 }
 

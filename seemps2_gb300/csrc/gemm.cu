@@ -122,9 +122,32 @@ int gemm(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const 
     return SM_ERR_VALUE;
   }
   k_gemm<T><<<grid, NT, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }
+
+template <typename T>
+int gemm_ctx(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A,
+             int lda, const T* B, int ldb, T beta, T* C, int ldc) {
+  if (M == 0 || N == 0 || K == 0) return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  ctx.stats.gemm_launches += 1;
+  ctx.stats.gemm_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
+  if (!ctx.timing) return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+  SM_CHECK(gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc));
+  SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+  SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
+  float ms = 0.f;
+  SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+  ctx.stats.gemm_ms += ms;
+  return SM_OK;
+}
+
+template int gemm_ctx<double>(Ctx&, cudaStream_t, int, int, int, int, int, double, const double*,
+                              int, const double*, int, double, double*, int);
+template int gemm_ctx<cplx>(Ctx&, cudaStream_t, int, int, int, int, int, cplx, const cplx*, int,
+                            const cplx*, int, cplx, cplx*, int);
 
 template int gemm<double>(cudaStream_t, int, int, int, int, int, double, const double*, int,
                           const double*, int, double, double*, int);

@@ -20,6 +20,9 @@ struct Ctx {
   std::map<std::string, std::pair<void*, size_t>> bufs;
   std::map<const void*, int> coop_blocks;  // per-kernel co-resident CTA limit
   // split trace (sm_trace_*): one record per SVD split, singular values included
+  sm_stats stats{};
+  bool timing = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool trace = false;
   std::vector<int> tr_rank, tr_len;
   std::vector<double> tr_err2, tr_s;
@@ -32,6 +35,10 @@ struct Ctx {
     return scratch(name, count * sizeof(P), reinterpret_cast<void**>(out));
   }
 };
+
+// Kernel launches issued by this library in this process (all contexts).
+void note_launch(int n = 1);
+long long launches_total();
 
 // Kept size and squared discarded weight of a split.
 struct SplitResult {
@@ -47,6 +54,11 @@ enum { OUT_NONE = 0, OUT_U = 1, OUT_US = 2 };
 enum { OUT_VT = 1, OUT_SVT = 2 };
 
 // --- gemm.cu ---------------------------------------------------------------
+// GEMM through the context: counts the launch and, when timing is enabled,
+// measures it with CUDA events.
+template <typename T>
+int gemm_ctx(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A,
+             int lda, const T* B, int ldb, T beta, T* C, int ldc);
 template <typename T>
 int gemm(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda,
          const T* B, int ldb, T beta, T* C, int ldc);

@@ -164,6 +164,7 @@ int scale_matrix(cudaStream_t st, int M, int N, T beta, T* C, int ldc) {
   const size_t n = (size_t)M * N;
   if (!n) return SM_OK;
   k_scale_matrix<T><<<grid_for<T>(n), 256, 0, st>>>(M, N, beta, C, ldc, S<T>::abs2(beta) == 0.0);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }
@@ -172,6 +173,7 @@ template <typename T>
 int scale_vector(cudaStream_t st, size_t n, double f, T* x) {
   if (!n) return SM_OK;
   k_scale_vector<T><<<grid_for<T>(n), 256, 0, st>>>(n, f, x);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }
@@ -189,6 +191,7 @@ int mpo_multiply_tensor(cudaStream_t st, const T* O, int a, int i, int j, int b,
   const size_t n = (size_t)c * a * i * d * b;
   if (!n) return SM_OK;
   k_mpo_multiply<T><<<grid_for<T>(n), 256, 0, st>>>(O, a, i, j, b, B, c, d, C);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }
@@ -199,8 +202,10 @@ int vdot(Ctx& ctx, cudaStream_t st, size_t n, const T* x, const T* y, double* ou
   SM_CHECK(ctx.scratch("vdot.part", 2 * kVdotBlocks, &part));
   const int nb = (int)std::max<size_t>(1, std::min<size_t>(kVdotBlocks, (n + 255) / 256));
   k_vdot_partial<T><<<nb, 256, 0, st>>>(n, x, y, part);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   k_vdot_final<<<1, 32, 0, st>>>(nb, part, out_dev);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }
@@ -210,6 +215,7 @@ int transpose(cudaStream_t st, int m, int n, const T* A, int lda, T* B, int ldb)
   if (!m || !n) return SM_OK;
   dim3 grid((n + 31) / 32, (m + 31) / 32);
   k_transpose<T><<<grid, dim3(32, 8), 0, st>>>(m, n, A, lda, B, ldb);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }
@@ -218,6 +224,7 @@ template <typename T>
 int set_identity(cudaStream_t st, int k, T* X, int ldx) {
   if (!k) return SM_OK;
   k_identity<T><<<grid_for<T>((size_t)k * k), 256, 0, st>>>(k, X, ldx);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }
@@ -228,6 +235,7 @@ int copy_block3(cudaStream_t st, const T* src, int a, int d, int b, T* dst, int 
   const size_t n = (size_t)a * d * b;
   if (!n) return SM_OK;
   k_copy_block3<T><<<grid_for<T>(n), 256, 0, st>>>(src, a, d, b, dst, A, B, off_a, off_b, w);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
 }

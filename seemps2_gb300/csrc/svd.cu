@@ -158,18 +158,34 @@ template <> struct Rot<cplx> {
   }
 };
 
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_jacobi(T* W, int ldw, T* X, int ldx, int k, int l,
-                                               double tol, int max_sweeps, JacobiCtl* ctl) {
-  __shared__ double red[4][NT / 32];
-  __shared__ double coef[4];
-  __shared__ int do_rot;
-  __shared__ unsigned int nrot_shared;
+// One warp per pair.  Each row is [w | x]: the l entries of the vector being
+// orthogonalised followed by the k entries of its row of the accumulated
+// unitary X, so one rotation updates both in a single pass.  With E > 0 a lane
+// keeps its E elements of both rows in registers between the dot product and
+// the rotation; E == 0 streams the rows twice from L2 (large sizes).
+//
+// Rotation parameters: only what must be exact is FP64.  The convergence test
+// |g|^2 > tol^2 a b needs no root; the angle t = tan(theta) is evaluated in
+// FP32 (an inexact angle only leaves a slightly larger residual for the next
+// sweep), while c = 1/sqrt(1+t^2), s = c t and the phase g/|g| use FP64 rsqrt,
+// so every applied rotation is unitary to FP64 rounding.  Squared norms are
+// computed exactly in the first round of every sweep and updated in closed
+// form after each rotation during the sweep.
+template <typename T, int E>
+__global__ void __launch_bounds__(256) k_jacobi(T* Wx, int ld, int k, int l, double tol2,
+                                                int max_sweeps, double* nrm, JacobiCtl* ctl) {
+  __shared__ int sflag;
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const int gw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  const int nw = gridDim.x * wpb;
   const int kp = k + (k & 1);
   const int rounds = kp - 1, npairs = kp / 2;
+  const int L = l + k;
+  volatile int* vflag = reinterpret_cast<volatile int*>(ctl->rot);
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int r = 0; r < rounds; ++r) {
-      for (int t = blockIdx.x; t < npairs; t += gridDim.x) {
+      for (int t = gw; t < npairs; t += nw) {
         int p, q;
         if (t == 0) {
           p = kp - 1;
@@ -178,66 +194,124 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* W, int ldw, T* X, int ldx, int
           p = (r + t) % (kp - 1);
           q = (r + kp - 1 - t) % (kp - 1);
         }
-        if (p >= k || q >= k) continue;  // the dummy player of an odd k
+        if (p >= k || q >= k) {
+          // the dummy player of an odd k: its partner idles this round, but
+          // in the first round its exact squared norm must still be refreshed
+          if (r == 0) {
+            const int row = p < q ? p : q;
+            double a = 0.0;
+            for (int x = lane; x < l; x += 32) a += S<T>::abs2(ldcg(Wx + (size_t)row * ld + x));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if (lane == 0) __stcg(nrm + row, a);
+          }
+          continue;
+        }
         if (p > q) { const int tmp = p; p = q; q = tmp; }
-        T* wp = W + (size_t)p * ldw;
-        T* wq = W + (size_t)q * ldw;
-        double a = 0.0, b = 0.0, gr = 0.0, gi = 0.0;
+        T* rp = Wx + (size_t)p * ld;
+        T* rq = Wx + (size_t)q * ld;
+        double a = 0.0, b = 0.0;
         T g = S<T>::zero();
-        for (int x = threadIdx.x; x < l; x += NT) {
-          const T u = ldcg(wp + x), v = ldcg(wq + x);
-          a += S<T>::abs2(u);
-          b += S<T>::abs2(v);
-          g = S<T>::cfma(u, v, g);
+        T u[E > 0 ? E : 1], v[E > 0 ? E : 1];
+        if constexpr (E > 0) {
+#pragma unroll
+          for (int e = 0; e < E; ++e) {
+            const int x = lane + 32 * e;
+            if (x < L) {
+              u[e] = ldcg(rp + x);
+              v[e] = ldcg(rq + x);
+            } else {
+              u[e] = S<T>::zero();
+              v[e] = S<T>::zero();
+            }
+            if (x < l) {
+              if (r == 0) {
+                a += S<T>::abs2(u[e]);
+                b += S<T>::abs2(v[e]);
+              }
+              g = S<T>::cfma(u[e], v[e], g);
+            }
+          }
+        } else {
+          for (int x = lane; x < l; x += 32) {
+            const T uu = ldcg(rp + x), vv = ldcg(rq + x);
+            if (r == 0) {
+              a += S<T>::abs2(uu);
+              b += S<T>::abs2(vv);
+            }
+            g = S<T>::cfma(uu, vv, g);
+          }
         }
+        double gr, gi;
         gamma_parts(g, gr, gi);
-        block_sum4<NT>(a, b, gr, gi, red);
-        if (threadIdx.x == 0) {
-          const double gabs = sqrt(gr * gr + gi * gi);
-          int rot = (gabs > 0.0) && (gabs > tol * sqrt(a) * sqrt(b));
-          if (rot) {
-            const double zeta = (b - a) / (2.0 * gabs);
-            double t;
-            if (fabs(zeta) > 1e150) t = 0.5 / zeta;
-            else t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-            const double c = 1.0 / sqrt(1.0 + t * t);
-            coef[0] = c;
-            coef[1] = c * t;
-            coef[2] = gr / gabs;
-            coef[3] = gi / gabs;
-            atomicAdd(&ctl->rot[sweep & 1], 1u);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          gr += __shfl_xor_sync(0xffffffffu, gr, o);
+          gi += __shfl_xor_sync(0xffffffffu, gi, o);
+          if (r == 0) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
           }
-          do_rot = rot;
         }
-        __syncthreads();
-        if (do_rot) {
+        if (r != 0) {
+          a = __ldcg(nrm + p);
+          b = __ldcg(nrm + q);
+        }
+        const double g2 = gr * gr + gi * gi;
+        const bool rot = g2 > 0.0 && g2 > tol2 * a * b;
+        double na = a, nb = b;
+        if (rot) {
+          const double rsq = rsqrt(g2);  // 1/|g|
+          const double gabs = g2 * rsq;
+          const double zeta = 0.5 * (b - a) * rsq;
+          double tt;
+          if (fabs(zeta) < 1e30) {
+            const float zf = (float)zeta;
+            const float az = fabsf(zf);
+            float tf = az > 1e18f ? 0.5f / az : 1.0f / (az + sqrtf(fmaf(az, az, 1.0f)));
+            tt = (double)copysignf(tf, zf);
+          } else {
+            tt = 0.5 / zeta;
+          }
+          const double c = rsqrt(fma(tt, tt, 1.0));
+          const double sn = c * tt;
           Rot<T> R;
-          R.set(coef[0], coef[1], coef[2], coef[3]);
-          for (int x = threadIdx.x; x < l; x += NT) {
-            T u = ldcg(wp + x), v = ldcg(wq + x);
-            R.apply(u, v);
-            stcg(wp + x, u);
-            stcg(wq + x, v);
+          R.set(c, sn, gr * rsq, gi * rsq);
+          const double cs2 = 2.0 * c * sn * gabs;
+          na = c * c * a + sn * sn * b - cs2;
+          nb = sn * sn * a + c * c * b + cs2;
+          if constexpr (E > 0) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+              const int x = lane + 32 * e;
+              R.apply(u[e], v[e]);
+              if (x < L) {
+                stcg(rp + x, u[e]);
+                stcg(rq + x, v[e]);
+              }
+            }
+          } else {
+            for (int x = lane; x < L; x += 32) {
+              T uu = ldcg(rp + x), vv = ldcg(rq + x);
+              R.apply(uu, vv);
+              stcg(rp + x, uu);
+              stcg(rq + x, vv);
+            }
           }
-          T* xp = X + (size_t)p * ldx;
-          T* xq = X + (size_t)q * ldx;
-          for (int x = threadIdx.x; x < k; x += NT) {
-            T u = ldcg(xp + x), v = ldcg(xq + x);
-            R.apply(u, v);
-            stcg(xp + x, u);
-            stcg(xq + x, v);
-          }
+          if (lane == 0) vflag[sweep & 1] = 1;
         }
-        __syncthreads();
+        if (lane == 0 && (rot || r == 0)) {
+          __stcg(nrm + p, na);
+          __stcg(nrm + q, nb);
+        }
       }
       if (!grid_sync(ctl)) return;
       // slot (sweep+1)&1 was read by every CTA before this barrier: recycle it
-      if (r == 0 && sweep > 0 && blockIdx.x == 0 && threadIdx.x == 0)
-        ctl->rot[(sweep + 1) & 1] = 0u;
+      if (r == 0 && sweep > 0 && blockIdx.x == 0 && threadIdx.x == 0) vflag[(sweep + 1) & 1] = 0;
     }
-    if (threadIdx.x == 0) nrot_shared = ((volatile unsigned int*)ctl->rot)[sweep & 1];
+    if (threadIdx.x == 0) sflag = vflag[sweep & 1];
     __syncthreads();
-    if (nrot_shared == 0u) {
+    if (sflag == 0) {
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->sweeps = sweep + 1;
       return;
     }
@@ -397,21 +471,73 @@ __global__ void k_emit(int wide, int m, int n, int D, const T* __restrict__ W, i
   }
 }
 
-constexpr int kJacobiThreads = 128;
 constexpr int kMaxSweeps = 60;
 
-template <typename T>
-int coop_limit(Ctx& ctx) {
-  const void* fn = reinterpret_cast<const void*>(&k_jacobi<T, kJacobiThreads>);
-  auto it = ctx.coop_blocks.find(fn);
-  if (it != ctx.coop_blocks.end()) return it->second;
+template <typename T, int E>
+int launch_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double tol2,
+                  double* nrm, JacobiCtl* ctl) {
+  const int npairs = (k + (k & 1)) / 2;
+  const int sms = std::max(1, ctx.num_sms);
+  const int wpb = std::min(8, std::max(1, (npairs + sms - 1) / sms));
+  const int threads = 32 * wpb;
+  auto fn = k_jacobi<T, E>;
+  const void* key = reinterpret_cast<const void*>(fn);
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi<T, kJacobiThreads>,
-                                                    kJacobiThreads, 0) != cudaSuccess)
-    per_sm = 1;
-  const int lim = std::max(1, per_sm) * std::max(1, ctx.num_sms);
-  ctx.coop_blocks[fn] = lim;
-  return lim;
+  const auto it = ctx.coop_blocks.find(key);
+  // occupancy depends on the block size; cache per (kernel, wpb)
+  const void* ckey = reinterpret_cast<const char*>(key) + wpb;
+  const auto it2 = ctx.coop_blocks.find(ckey);
+  (void)it;
+  if (it2 != ctx.coop_blocks.end()) per_sm = it2->second;
+  else {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess)
+      per_sm = 1;
+    per_sm = std::max(1, per_sm);
+    ctx.coop_blocks[ckey] = per_sm;
+  }
+  const int grid = std::max(1, std::min((npairs + wpb - 1) / wpb, per_sm * sms));
+  int ms = kMaxSweeps;
+  void* args[] = {&Wx, &ld, &k, &l, &tol2, &ms, &nrm, &ctl};
+  SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
+                                            dim3(threads), args, 0, st));
+                                            note_launch();
+  return SM_OK;
+}
+
+template <typename T>
+int run_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, double* nrm,
+               JacobiCtl* ctl) {
+  const int L = l + k;
+  const int need = (L + 31) / 32;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (need <= 2) return launch_jacobi<T, 2>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 4) return launch_jacobi<T, 4>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 8) return launch_jacobi<T, 8>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 12) return launch_jacobi<T, 12>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 16) return launch_jacobi<T, 16>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 24) return launch_jacobi<T, 24>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 32) return launch_jacobi<T, 32>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 40) return launch_jacobi<T, 40>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+  } else {
+    if (need <= 2) return launch_jacobi<T, 2>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 4) return launch_jacobi<T, 4>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 8) return launch_jacobi<T, 8>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 12) return launch_jacobi<T, 12>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 16) return launch_jacobi<T, 16>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+    if (need <= 20) return launch_jacobi<T, 20>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+  }
+  return launch_jacobi<T, 0>(ctx, st, Wx, ld, k, l, tol2, nrm, ctl);
+}
+
+template <typename T>
+__global__ void k_fill_rows(int k, int l, T* Wx, int ld) {
+  // X part of [W | X] = identity
+  const size_t total = (size_t)k * k;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / k), j = (int)(e % k);
+    Wx[(size_t)i * ld + l + j] = i == j ? S<T>::one() : S<T>::zero();
+  }
 }
 
 }  // namespace
@@ -423,6 +549,7 @@ int truncate_device(Ctx& ctx, cudaStream_t st, const double* s_dev, int n,
   SM_CHECK(ctx.scratch("trunc.errors", (size_t)n + 1, &errors));
   SM_CHECK(ctx.scratch("trunc.res", 1, &res));
   k_truncate<<<1, 32, 0, st>>>(s_dev, n, strat, errors, res);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   SplitResult* h = reinterpret_cast<SplitResult*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(h, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
@@ -442,13 +569,13 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
   }
   const int k = std::min(m, n), l = std::max(m, n);
   const bool wide = m <= n;
-  T *W, *X;
+  const int ld = l + k;  // rows are [w (l) | x (k)]
+  T* Wx;
   double *nrm, *s_sorted, *errors;
   int* perm;
   JacobiCtl* ctl;
   SplitResult* res;
-  SM_CHECK(ctx.scratch("svd.W", (size_t)k * l, &W));
-  SM_CHECK(ctx.scratch("svd.X", (size_t)k * k, &X));
+  SM_CHECK(ctx.scratch("svd.Wx", (size_t)k * ld, &Wx));
   SM_CHECK(ctx.scratch("svd.nrm", (size_t)k, &nrm));
   SM_CHECK(ctx.scratch("svd.s", (size_t)k, &s_sorted));
   SM_CHECK(ctx.scratch("svd.err", (size_t)k + 1, &errors));
@@ -457,23 +584,31 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
   SM_CHECK(ctx.scratch("svd.res", 1, &res));
 
   if (wide) {
-    SM_CUDA_CHECK(cudaMemcpyAsync(W, A, sizeof(T) * (size_t)k * l, cudaMemcpyDeviceToDevice, st));
+    SM_CUDA_CHECK(cudaMemcpy2DAsync(Wx, sizeof(T) * ld, A, sizeof(T) * n, sizeof(T) * n, m,
+                                    cudaMemcpyDeviceToDevice, st));
   } else {
-    SM_CHECK(transpose<T>(st, m, n, A, n, W, m));
+    SM_CHECK(transpose<T>(st, m, n, A, n, Wx, ld));
   }
-  SM_CHECK(set_identity<T>(st, k, X, k));
+  {
+    const size_t tot = (size_t)k * k;
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, 4096));
+    k_fill_rows<T><<<blocks, 256, 0, st>>>(k, l, Wx, ld);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+  }
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
   if (k >= 2) {
-    const int npairs = (k + (k & 1)) / 2;
-    const int grid = std::min(npairs, coop_limit<T>(ctx));
-    int ldw = l, ldx = k, kk = k, ll = l, ms = kMaxSweeps;
-    double tol = std::sqrt((double)l) * DBL_EPSILON;
-    void* args[] = {&W, &ldw, &X, &ldx, &kk, &ll, &tol, &ms, &ctl};
-    SM_CUDA_CHECK(cudaLaunchCooperativeKernel(
-        reinterpret_cast<const void*>(&k_jacobi<T, kJacobiThreads>), dim3(grid),
-        dim3(kJacobiThreads), args, 0, st));
+    const double tol = std::sqrt((double)l) * DBL_EPSILON;
+    if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+    SM_CHECK(run_jacobi<T>(ctx, st, Wx, ld, k, l, tol * tol, nrm, ctl));
+    if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+    ctx.stats.jacobi_launches += 1;
+    // 4 m n^2 + 8 n^3 with m >= n (x4 for complex arithmetic)
+    ctx.stats.jacobi_flops += (4.0 * l * (double)k * k + 8.0 * (double)k * k * k) *
+                              (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
   }
-  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(W, l, k, l, nrm);
+  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   const size_t smem = sizeof(unsigned long long) * (size_t)k;
   if (smem > 200 * 1024) {
@@ -484,11 +619,19 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
   k_sort_truncate<<<1, 1024, smem, st>>>(nrm, k, strat, perm, s_sorted, errors, ctl, res);
+  note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   SplitResult* h = reinterpret_cast<SplitResult*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(h, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
   *out = *h;
+  ctx.stats.splits += 1;
+  ctx.stats.jacobi_sweeps += h->sweeps;
+  if (ctx.timing && k >= 2) {
+    float ms = 0.f;
+    SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+    ctx.stats.jacobi_ms += ms;
+  }
   if (h->status & DEV_BARRIER_TIMEOUT) {
     set_error("svd: grid barrier timed out");
     return SM_ERR_TIMEOUT;
@@ -517,8 +660,9 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
   if (left_mode || right_mode) {
     const size_t total = (left_mode ? (size_t)m * D : 0) + (right_mode ? (size_t)D * n : 0);
     const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
-    k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(wide, m, n, D, W, l, X, k, perm, s_sorted,
-                                                   left_mode, left, right_mode, right);
+    k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(wide, m, n, D, Wx, ld, Wx + l, ld, perm,
+                                                   s_sorted, left_mode, left, right_mode, right);
+                                                   note_launch();
     SM_CUDA_CHECK(cudaGetLastError());
   }
   return SM_OK;

@@ -65,7 +65,7 @@ struct Sweeper {
   // ---- helpers -------------------------------------------------------------
   int gemm_(int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda, const T* B,
             int ldb, T beta, T* C, int ldc) {
-    return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    return gemm_ctx<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   }
   static T one() { return S<T>::one(); }
   static T zero() { return S<T>::zero(); }
