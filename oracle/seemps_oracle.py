@@ -162,6 +162,9 @@ def truncate(s: np.ndarray, strategy: Strategy) -> tuple[int, float]:
 # --------------------------------------------------------------------------
 
 
+GESDD_RETRIES = [0]
+
+
 def svd(A: np.ndarray):
     """Economy SVD through LAPACK ?gesdd called directly, as the reference's
     Cython core does (svd.pxi:35-83, gesdd being its default driver :23)."""
@@ -171,6 +174,14 @@ def svd(A: np.ndarray):
         A = A.astype(np.float64)
     f = scipy.linalg.lapack.zgesdd if np.iscomplexobj(A) else scipy.linalg.lapack.dgesdd
     U, s, Vh, info = f(A, compute_uv=1, full_matrices=0)
+    if info > 0:
+        # Some LAPACK builds (seen with OpenBLAS on aarch64) report that the
+        # divide-and-conquer stage did not converge on matrices that gesvd
+        # handles; the reference offers gesvd as its other driver
+        # (svd.pxi:25-32).  The retry is counted so callers can report it.
+        GESDD_RETRIES[0] += 1
+        g = scipy.linalg.lapack.zgesvd if np.iscomplexobj(A) else scipy.linalg.lapack.dgesvd
+        U, s, Vh, info = g(A, compute_uv=1, full_matrices=0)
     if info > 0:
         raise np.linalg.LinAlgError("SVD did not converge")
     if info < 0:
