@@ -160,40 +160,52 @@ template <> struct Rot<cplx> {
   }
 };
 
-// One warp per pair.  Each row is [w | x]: the l entries of the vector being
+// One CTA (NT threads, NT/32 warps) per pair, so that every SM sub-partition's
+// FP64 unit works on a pair (GB300 FP64 is latency-bound with one warp per
+// pair).  Each row is [w | x]: the l entries of the vector being
 // orthogonalised followed by the k entries of its row of the accumulated
-// unitary X, so one rotation updates both in a single pass.  With E > 0 a lane
-// keeps its E elements of both rows in registers between the dot product and
-// the rotation; E == 0 streams the rows twice from L2 (large sizes).
+// unitary X, so one rotation updates both in a single pass.  With E > 0 a
+// thread keeps its E elements of both rows in registers between the dot
+// products and the rotation; E == 0 streams the rows twice from L2.
 //
-// Rotation parameters avoid FP64 division and square roots (slow on GB300's
-// FP64 unit): the convergence test |g|^2 > tol^2 a b needs no root, and the
-// angle, c = 1/sqrt(1+t^2), s = c t and the phase g/|g| use the FP64 rsqrt and
-// reciprocal intrinsics, so every applied rotation is unitary to FP64
-// rounding.  Squared norms are computed exactly in the first round of every
-// sweep and updated in closed form after each rotation during the sweep.
-template <typename T, int E>
-__global__ void __launch_bounds__(256) k_jacobi(T* Wx, int ld, int k, int l, double tol2,
-                                                int max_sweeps, double* nrm, const double* nrm0,
-                                                JacobiCtl* ctl) {
+// Rotation parameters: the convergence test |g|^2 > tol^2 a b needs no root;
+// zeta = (b - a) / 2|g| uses one FP64 rsqrt; t = tan(theta) is evaluated in
+// FP32 (an inexact angle only leaves a slightly larger residual for the next
+// sweep) except for |zeta| >= 1e18 where t = 1/2zeta in FP64; c = 1/sqrt(1+t^2),
+// s = c t and the complex phase g/|g| use FP64 rsqrt, so every applied rotation
+// is unitary to FP64 rounding.  Squared norms are computed exactly in the first
+// round of every sweep and updated in closed form after each rotation.
+//
+// Pairs whose overlap is below an absolute floor (16 l eps^2 |A|_F^2, just
+// above the rounding-noise level) count as orthogonal when `use_floor` is set:
+// the noise vectors of a numerically rank-deficient matrix are then not
+// rotated against each other sweep after sweep.  The caller sets it only when
+// the truncation rule is certain to discard every such vector.
+template <typename T, int NT, int E>
+__global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, double tol2,
+                                               int use_floor, int max_sweeps, double* nrm,
+                                               const double* nrm0, JacobiCtl* ctl) {
+  constexpr int NW = NT / 32;
+  __shared__ double part[2][NW][4];
   __shared__ int sflag;
-  const int lane = threadIdx.x & 31;
-  const int wpb = blockDim.x >> 5;
-  const int gw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  const int nw = gridDim.x * wpb;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int kp = k + (k & 1);
   const int rounds = kp - 1, npairs = kp / 2;
   const int L = l + k;
   volatile int* vflag = reinterpret_cast<volatile int*>(ctl->rot);
-  double frob2 = 0.0;  // |A|_F^2 from the squared row norms, fixed order
-  for (int i = lane; i < k; i += 32) frob2 += __ldcg(nrm0 + i);
+  double tiny2 = 0.0;
+  if (use_floor) {
+    double frob2 = 0.0;  // |A|_F^2 from the squared row norms, fixed order
+    for (int i = lane; i < k; i += 32) frob2 += __ldcg(nrm0 + i);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) frob2 += __shfl_xor_sync(0xffffffffu, frob2, o);
-  const double tiny = 256.0 * l * DBL_EPSILON * DBL_EPSILON * frob2;
-  const double tiny2 = tiny * tiny;
+    for (int o = 16; o > 0; o >>= 1) frob2 += __shfl_xor_sync(0xffffffffu, frob2, o);
+    const double tiny = 16.0 * l * DBL_EPSILON * DBL_EPSILON * frob2;
+    tiny2 = tiny * tiny;
+  }
+  int it = 0;  // pair iterations of this CTA (selects the smem buffer)
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int r = 0; r < rounds; ++r) {
-      for (int t = gw; t < npairs; t += nw) {
+      for (int t = blockIdx.x; t < npairs; t += gridDim.x, ++it) {
         int p, q;
         if (t == 0) {
           p = kp - 1;
@@ -202,16 +214,23 @@ __global__ void __launch_bounds__(256) k_jacobi(T* Wx, int ld, int k, int l, dou
           p = (r + t) % (kp - 1);
           q = (r + kp - 1 - t) % (kp - 1);
         }
+        double (*pt)[4] = part[it & 1];
         if (p >= k || q >= k) {
           // the dummy player of an odd k: its partner idles this round, but
           // in the first round its exact squared norm must still be refreshed
           if (r == 0) {
             const int row = p < q ? p : q;
             double a = 0.0;
-            for (int x = lane; x < l; x += 32) a += S<T>::abs2(ldcg(Wx + (size_t)row * ld + x));
+            for (int x = tid; x < l; x += NT) a += S<T>::abs2(ldcg(Wx + (size_t)row * ld + x));
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-            if (lane == 0) __stcg(nrm + row, a);
+            if (lane == 0) pt[warp][0] = a;
+            __syncthreads();
+            if (tid == 0) {
+              double s = 0.0;
+              for (int w = 0; w < NW; ++w) s += pt[w][0];
+              __stcg(nrm + row, s);
+            }
           }
           continue;
         }
@@ -219,12 +238,12 @@ __global__ void __launch_bounds__(256) k_jacobi(T* Wx, int ld, int k, int l, dou
         T* rp = Wx + (size_t)p * ld;
         T* rq = Wx + (size_t)q * ld;
         double a = 0.0, b = 0.0;
-        T g = S<T>::zero();
+        T g0 = S<T>::zero(), g1 = S<T>::zero();
         T u[E > 0 ? E : 1], v[E > 0 ? E : 1];
         if constexpr (E > 0) {
 #pragma unroll
           for (int e = 0; e < E; ++e) {
-            const int x = lane + 32 * e;
+            const int x = tid + NT * e;
             if (x < L) {
               u[e] = ldcg(rp + x);
               v[e] = ldcg(rq + x);
@@ -232,26 +251,34 @@ __global__ void __launch_bounds__(256) k_jacobi(T* Wx, int ld, int k, int l, dou
               u[e] = S<T>::zero();
               v[e] = S<T>::zero();
             }
+          }
+#pragma unroll
+          for (int e = 0; e < E; ++e) {
+            const int x = tid + NT * e;
             if (x < l) {
               if (r == 0) {
                 a += S<T>::abs2(u[e]);
                 b += S<T>::abs2(v[e]);
               }
-              g = S<T>::cfma(u[e], v[e], g);
+              if (e & 1) g1 = S<T>::cfma(u[e], v[e], g1);
+              else g0 = S<T>::cfma(u[e], v[e], g0);
             }
           }
         } else {
-          for (int x = lane; x < l; x += 32) {
+          for (int x = tid; x < l; x += NT) {
             const T uu = ldcg(rp + x), vv = ldcg(rq + x);
             if (r == 0) {
               a += S<T>::abs2(uu);
               b += S<T>::abs2(vv);
             }
-            g = S<T>::cfma(uu, vv, g);
+            g0 = S<T>::cfma(uu, vv, g0);
           }
         }
-        double gr, gi;
-        gamma_parts(g, gr, gi);
+        double gr, gi, hr, hi;
+        gamma_parts(g0, gr, gi);
+        gamma_parts(g1, hr, hi);
+        gr += hr;
+        gi += hi;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
           gr += __shfl_xor_sync(0xffffffffu, gr, o);
@@ -261,43 +288,61 @@ __global__ void __launch_bounds__(256) k_jacobi(T* Wx, int ld, int k, int l, dou
             b += __shfl_xor_sync(0xffffffffu, b, o);
           }
         }
+        if (lane == 0) {
+          pt[warp][0] = gr;
+          pt[warp][1] = gi;
+          pt[warp][2] = a;
+          pt[warp][3] = b;
+        }
+        __syncthreads();
+        gr = gi = 0.0;
+        if (r == 0) a = b = 0.0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {  // same order in every thread
+          gr += pt[w][0];
+          gi += pt[w][1];
+          if (r == 0) {
+            a += pt[w][2];
+            b += pt[w][3];
+          }
+        }
         if (r != 0) {
           a = __ldcg(nrm + p);
           b = __ldcg(nrm + q);
         }
         const double g2 = gr * gr + gi * gi;
-        // relative test |g| > tol sqrt(a b), plus an absolute floor just above
-        // the rounding-noise level (256 l eps^2 |A|_F^2): the noise vectors of a
-        // numerically rank-deficient matrix are not rotated against each other
-        // sweep after sweep, while every vector with a norm above
-        // 16 sqrt(l) eps |A| (~1e-13 |A|) is still fully orthogonalised
         const bool rot = g2 > tiny2 && g2 > tol2 * a * b;
         double na = a, nb = b;
         if (rot) {
           const double rsq = rsqrt(g2);  // 1/|g|
-          const double gabs = g2 * rsq;
           const double zeta = 0.5 * (b - a) * rsq;
-          // t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)), the smaller root
-          const double az = fabs(zeta);
           double tt;
-          if (az < 1e150) {
-            const double w = fma(az, az, 1.0);
-            tt = __drcp_rn(az + w * rsqrt(w));
+          if (fabs(zeta) < 1e18) {
+            const float zf = (float)zeta;
+            const float az = fabsf(zf);
+            tt = (double)copysignf(1.0f / (az + sqrtf(fmaf(az, az, 1.0f))), zf);
           } else {
-            tt = __drcp_rn(2.0 * az);
+            tt = __drcp_rn(2.0 * zeta);
           }
-          tt = copysign(tt, zeta);
           const double c = rsqrt(fma(tt, tt, 1.0));
           const double sn = c * tt;
+          double er, ei;
+          if constexpr (sizeof(T) == sizeof(double)) {
+            er = gr >= 0.0 ? 1.0 : -1.0;  // the phase of a real overlap is its sign
+            ei = 0.0;
+          } else {
+            er = gr * rsq;
+            ei = gi * rsq;
+          }
           Rot<T> R;
-          R.set(c, sn, gr * rsq, gi * rsq);
-          const double cs2 = 2.0 * c * sn * gabs;
-          na = c * c * a + sn * sn * b - cs2;
-          nb = sn * sn * a + c * c * b + cs2;
+          R.set(c, sn, er, ei);
+          const double cs2 = 2.0 * c * sn * (g2 * rsq);
+          na = fma(c * c, a, fma(sn * sn, b, -cs2));
+          nb = fma(sn * sn, a, fma(c * c, b, cs2));
           if constexpr (E > 0) {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-              const int x = lane + 32 * e;
+              const int x = tid + NT * e;
               R.apply(u[e], v[e]);
               if (x < L) {
                 stcg(rp + x, u[e]);
@@ -305,32 +350,32 @@ __global__ void __launch_bounds__(256) k_jacobi(T* Wx, int ld, int k, int l, dou
               }
             }
           } else {
-            for (int x = lane; x < L; x += 32) {
+            for (int x = tid; x < L; x += NT) {
               T uu = ldcg(rp + x), vv = ldcg(rq + x);
               R.apply(uu, vv);
               stcg(rp + x, uu);
               stcg(rq + x, vv);
             }
           }
-          if (lane == 0) vflag[sweep & 1] = 1;
+          if (tid == 0) vflag[sweep & 1] = 1;
         }
-        if (lane == 0 && (rot || r == 0)) {
+        if (tid == 0 && (rot || r == 0)) {
           __stcg(nrm + p, na);
           __stcg(nrm + q, nb);
         }
       }
       if (!grid_sync(ctl)) return;
       // slot (sweep+1)&1 was read by every CTA before this barrier: recycle it
-      if (r == 0 && sweep > 0 && blockIdx.x == 0 && threadIdx.x == 0) vflag[(sweep + 1) & 1] = 0;
+      if (r == 0 && sweep > 0 && blockIdx.x == 0 && tid == 0) vflag[(sweep + 1) & 1] = 0;
     }
-    if (threadIdx.x == 0) sflag = vflag[sweep & 1];
+    if (tid == 0) sflag = vflag[sweep & 1];
     __syncthreads();
     if (sflag == 0) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) ctl->sweeps = sweep + 1;
+      if (blockIdx.x == 0 && tid == 0) ctl->sweeps = sweep + 1;
       return;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (blockIdx.x == 0 && tid == 0) {
     ctl->sweeps = max_sweeps;
     atomicOr(&ctl->status, DEV_NOT_CONVERGED);
   }
@@ -487,60 +532,56 @@ __global__ void k_emit(int wide, int m, int n, int D, const T* __restrict__ W, i
 
 constexpr int kMaxSweeps = 60;
 
+constexpr int kJacobiNT = 128;
+
 template <typename T, int E>
 int launch_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double tol2,
-                  double* nrm, const double* nrm0, JacobiCtl* ctl) {
+                  int use_floor, double* nrm, const double* nrm0, JacobiCtl* ctl) {
   const int npairs = (k + (k & 1)) / 2;
   const int sms = std::max(1, ctx.num_sms);
-  const int wpb = std::min(8, std::max(1, (npairs + sms - 1) / sms));
-  const int threads = 32 * wpb;
-  auto fn = k_jacobi<T, E>;
+  auto fn = k_jacobi<T, kJacobiNT, E>;
   const void* key = reinterpret_cast<const void*>(fn);
   int per_sm = 0;
   const auto it = ctx.coop_blocks.find(key);
-  // occupancy depends on the block size; cache per (kernel, wpb)
-  const void* ckey = reinterpret_cast<const char*>(key) + wpb;
-  const auto it2 = ctx.coop_blocks.find(ckey);
-  (void)it;
-  if (it2 != ctx.coop_blocks.end()) per_sm = it2->second;
+  if (it != ctx.coop_blocks.end()) per_sm = it->second;
   else {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kJacobiNT, 0) != cudaSuccess)
       per_sm = 1;
     per_sm = std::max(1, per_sm);
-    ctx.coop_blocks[ckey] = per_sm;
+    ctx.coop_blocks[key] = per_sm;
   }
-  const int grid = std::max(1, std::min((npairs + wpb - 1) / wpb, per_sm * sms));
+  const int grid = std::max(1, std::min(npairs, per_sm * sms));
   int ms = kMaxSweeps;
-  void* args[] = {&Wx, &ld, &k, &l, &tol2, &ms, &nrm, &nrm0, &ctl};
+  void* args[] = {&Wx, &ld, &k, &l, &tol2, &use_floor, &ms, &nrm, &nrm0, &ctl};
   SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
-                                            dim3(threads), args, 0, st));
-                                            note_launch();
+                                            dim3(kJacobiNT), args, 0, st));
+  note_launch();
   return SM_OK;
 }
 
 template <typename T>
-int run_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, double* nrm,
-               const double* nrm0, JacobiCtl* ctl) {
-  const int L = l + k;
-  const int need = (L + 31) / 32;
+int run_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
+               double* nrm, const double* nrm0, JacobiCtl* ctl) {
+  const int need = (l + k + kJacobiNT - 1) / kJacobiNT;
+#define SM_J(EV) return launch_jacobi<T, EV>(ctx, st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl)
   if constexpr (sizeof(T) == sizeof(double)) {
-    if (need <= 2) return launch_jacobi<T, 2>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 4) return launch_jacobi<T, 4>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 8) return launch_jacobi<T, 8>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 12) return launch_jacobi<T, 12>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 16) return launch_jacobi<T, 16>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 24) return launch_jacobi<T, 24>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 32) return launch_jacobi<T, 32>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 40) return launch_jacobi<T, 40>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
+    if (need <= 1) SM_J(1);
+    if (need <= 2) SM_J(2);
+    if (need <= 4) SM_J(4);
+    if (need <= 6) SM_J(6);
+    if (need <= 8) SM_J(8);
+    if (need <= 10) SM_J(10);
+    if (need <= 12) SM_J(12);
+    if (need <= 16) SM_J(16);
   } else {
-    if (need <= 2) return launch_jacobi<T, 2>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 4) return launch_jacobi<T, 4>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 8) return launch_jacobi<T, 8>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 12) return launch_jacobi<T, 12>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 16) return launch_jacobi<T, 16>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
-    if (need <= 20) return launch_jacobi<T, 20>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
+    if (need <= 1) SM_J(1);
+    if (need <= 2) SM_J(2);
+    if (need <= 4) SM_J(4);
+    if (need <= 6) SM_J(6);
+    if (need <= 8) SM_J(8);
   }
-  return launch_jacobi<T, 0>(ctx, st, Wx, ld, k, l, tol2, nrm, nrm0, ctl);
+  SM_J(0);
+#undef SM_J
 }
 
 template <typename T>
@@ -613,6 +654,16 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     SM_CUDA_CHECK(cudaGetLastError());
   }
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
+  // The absolute floor leaves vectors with sigma^2 below ~16 l eps^2 |A|_F^2
+  // unorthogonalised among themselves; enable it only when the truncation
+  // rule certainly drops all of them (their summed weight is at most
+  // 16 k l eps^2 |A|_F^2).
+  const double eps = DBL_EPSILON;
+  bool use_floor = false;
+  if (strat.method == SM_RELATIVE_NORM_SQUARED_ERROR)
+    use_floor = strat.tolerance >= 64.0 * k * (double)l * eps * eps;
+  else if (strat.method == SM_RELATIVE_SINGULAR_VALUE)
+    use_floor = strat.tolerance >= 16.0 * std::sqrt((double)k * l) * eps;
   if (k >= 2) {
     // squared row norms -> nrm; the Jacobi kernel sums them into |A|_F^2
     k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm0, 1);
@@ -620,7 +671,7 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     SM_CUDA_CHECK(cudaGetLastError());
     const double tol = std::sqrt((double)l) * DBL_EPSILON;
     if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
-    SM_CHECK(run_jacobi<T>(ctx, st, Wx, ld, k, l, tol * tol, nrm, nrm0, ctl));
+    SM_CHECK(run_jacobi<T>(ctx, st, Wx, ld, k, l, tol * tol, use_floor ? 1 : 0, nrm, nrm0, ctl));
     if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
     ctx.stats.jacobi_launches += 1;
     // 4 m n^2 + 8 n^3 with m >= n (x4 for complex arithmetic)
