@@ -60,25 +60,35 @@ CASES = {
 }
 
 
+def _norm(mps) -> float:
+    """|psi| by a plain NumPy left-environment contraction (fixed, oracle-independent)."""
+    rho = np.eye(1)
+    for A in mps:
+        a, d, b = A.shape
+        t = (rho @ A.reshape(a, d * b)).reshape(a * d, b)
+        rho = A.reshape(a * d, b).conj().T @ t
+    return float(np.sqrt(abs(rho[0, 0].real)))
+
+
 def make_inputs(p: dict):
     rng = np.random.default_rng(p["seed"])
     n, d = p["n"], p["d"]
     if p["kind"] == "mpo_apply":
         mps = so.random_mps(d, n, p["chi"], rng, complex_=p["complex"])
-        nrm = np.sqrt(so.norm_squared(mps))
+        nrm = _norm(mps)
         mps = so.scale(mps, 1.0 / nrm)
         mpo = so.random_mpo(d, n, p["D"], rng, complex_=p["complex"])
         return mps, mpo
     if p["kind"] in ("laplacian", "euler"):
         mps = so.random_mps(d, n, p["chi"], rng, complex_=False)
-        nrm = np.sqrt(so.norm_squared(mps))
+        nrm = _norm(mps)
         mps = so.scale(mps, 1.0 / nrm)
         h = 2.0 ** (-n)
         mpo = so.tridiagonal_mpo(n, -2.0 / h**2, 1.0 / h**2, 1.0 / h**2)
         return mps, mpo
     if p["kind"] == "simplify":
         mps = so.random_mps(d, n, p["chi"], rng, complex_=p["complex"])
-        nrm = np.sqrt(so.norm_squared(mps))
+        nrm = _norm(mps)
         mps = so.scale(mps, 1.0 / nrm)
         return mps, None
     raise ValueError(p["kind"])
