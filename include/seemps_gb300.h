@@ -112,6 +112,21 @@ int sm_svd(void* ctx, int dtype, const void* A, int m, int n, void* U, double* s
 int sm_left_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int d2,
                        int b, const sm_strategy* st, void* U, void* SV, int* D,
                        double* err, void* stream);
+/* Allocation-free _left_orth_2site.  No counterpart in the reference: it is the
+ * same split as sm_left_orth_2site for callers that cannot allocate device
+ * memory while they run (host applications that own all device memory through
+ * their own pool, plugins that are only handed buffers, loops where a
+ * cudaMalloc would synchronise the device).  It needs no context and calls no
+ * cudaMalloc/cudaFree or allocating library routine: its intermediates live
+ * in a static device array (about 2 MiB, held by every GPU that loads the
+ * library until exit).  Limit: a*d1 <= 256 and d2*b <= 256, larger inputs
+ * return SM_ERR_VALUE.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's contents;
+ * calls that overlap on the GPU race on it, so serialise them. */
+int sm_left_orth_2site_noalloc(int dtype, const void* AA, int a, int d1, int d2, int b,
+                               const sm_strategy* st, void* U, void* SV, int* D,
+                               double* err, void* stream);
 /* _right_orth_2site (cython/schmidt.pxi:150-174): -> US[a,d1,D], V[D,d2,b]. */
 int sm_right_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int d2,
                         int b, const sm_strategy* st, void* US, void* V, int* D,

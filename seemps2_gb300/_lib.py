@@ -83,6 +83,8 @@ SIGNATURES = {
                                      vp, ip, dp, vp]),
     "sm_right_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,
                                       vp, ip, dp, vp]),
+    "sm_left_orth_2site_noalloc": (C.c_int, [C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp,
+                                             vp, vp, ip, dp, vp]),
     "sm_update_left_environment": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, C.c_int,
                                              C.c_int, vp, vp, vp]),
     "sm_update_right_environment": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp,

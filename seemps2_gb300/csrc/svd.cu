@@ -744,4 +744,197 @@ template int svd_split<double>(Ctx&, cudaStream_t, const double*, int, int, cons
 template int svd_split<cplx>(Ctx&, cudaStream_t, const cplx*, int, int, const sm_strategy&, int,
                              cplx*, int, cplx*, double*, SplitResult*);
 
+
+// ---------------------------------------------------------------------------
+// Allocation-free two-site split.
+//
+// Some callers cannot allocate device memory while they run: code embedded in
+// a host application that owns all device memory through its own pool, code
+// running where a cudaMalloc would synchronise the device or fail (inside a
+// latency-critical loop, under a memory cap), or plugins that are only handed
+// buffers.  For them sm_left_orth_2site_noalloc performs the same split as
+// sm_left_orth_2site with every intermediate array carved out of the static
+// device array below instead of the context's growable scratch.  The caller
+// still passes the input and the two output buffers.
+//
+// Limits: both matrix dimensions a*d1 and d2*b at most kNoAllocMaxDim (256);
+// the array then holds the [W | X] rows (at most 256 x 512 complex128
+// elements, 2 MiB) plus the per-row vectors.  Every GPU that loads the library
+// holds this array until the process exits.  All calls share it and it keeps
+// the previous call's contents (everything that must start at zero is cleared
+// by each call); calls whose work overlaps on the GPU (different streams,
+// different host threads) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocMaxDim = 256;
+constexpr size_t kNoAllocRowsBytes =
+    (size_t)kNoAllocMaxDim * (2 * kNoAllocMaxDim) * sizeof(cplx);  // [W | X], 2 MiB
+constexpr size_t kNoAllocVecBytes = 16 * 1024;                     // norms, order, control
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocRowsBytes + kNoAllocVecBytes];
+
+static unsigned char* g_noalloc_ptr[64];  // host copies of the array's device address, per device
+
+// One-time set-up per device (with that device current): the array's name is
+// only a host-side stand-in, the kernels need its device address.
+static int noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  SM_CUDA_CHECK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("noalloc: device ordinal out of range");
+    return SM_ERR_VALUE;
+  }
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    SM_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = reinterpret_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return SM_OK;
+}
+
+// Cooperative Jacobi launch without any cache (the context-based launcher
+// keeps occupancy results in a map; this one queries the runtime each time).
+template <typename T, int E>
+int launch_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
+                          double* nrm, const double* nrm0, JacobiCtl* ctl) {
+  const int npairs = (k + (k & 1)) / 2;
+  int dev = 0, sms = 1, per_sm = 1;
+  SM_CUDA_CHECK(cudaGetDevice(&dev));
+  SM_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  auto fn = k_jacobi<T, kJacobiNT, E>;
+  SM_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kJacobiNT, 0));
+  const int grid = std::max(1, std::min(npairs, std::max(1, per_sm) * std::max(1, sms)));
+  int ms = kMaxSweeps;
+  void* args[] = {&Wx, &ld, &k, &l, &tol2, &use_floor, &ms, &nrm, &nrm0, &ctl};
+  SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
+                                            dim3(kJacobiNT), args, 0, st));
+  note_launch();
+  return SM_OK;
+}
+
+template <typename T>
+int run_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
+                       double* nrm, const double* nrm0, JacobiCtl* ctl) {
+  // k <= 256 and l <= 256 here, so a thread holds at most 4 elements per row
+  const int need = (l + k + kJacobiNT - 1) / kJacobiNT;
+  if (need <= 1)
+    return launch_jacobi_noalloc<T, 1>(st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl);
+  if (need <= 2)
+    return launch_jacobi_noalloc<T, 2>(st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl);
+  return launch_jacobi_noalloc<T, 4>(st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl);
+}
+
+template <typename T>
+int left_orth_2site_noalloc(cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
+                            T* left, T* right, int* D_out, double* err_out) {
+  if (m <= 0 || n <= 0) {
+    set_error("noalloc split: empty matrix");
+    return SM_ERR_VALUE;
+  }
+  if (m > kNoAllocMaxDim || n > kNoAllocMaxDim) {
+    set_error("noalloc split: matrix " + std::to_string(m) + " x " + std::to_string(n) +
+              " exceeds the static scratch limit of " + std::to_string(kNoAllocMaxDim) +
+              " per dimension");
+    return SM_ERR_VALUE;
+  }
+  unsigned char* base;
+  SM_CHECK(noalloc_scratch(&base));
+  const int k = std::min(m, n), l = std::max(m, n);
+  const bool wide = m <= n;
+  const int ld = l + k;
+  T* Wx = reinterpret_cast<T*>(base);
+  unsigned char* v = base + kNoAllocRowsBytes;
+  double* nrm = reinterpret_cast<double*>(v);
+  double* nrm0 = nrm + kNoAllocMaxDim;
+  double* s_sorted = nrm0 + kNoAllocMaxDim;
+  double* errors = s_sorted + kNoAllocMaxDim;  // k + 1 entries
+  int* perm = reinterpret_cast<int*>(errors + kNoAllocMaxDim + 1);
+  JacobiCtl* ctl = reinterpret_cast<JacobiCtl*>(
+      reinterpret_cast<unsigned char*>(perm) + ((kNoAllocMaxDim * sizeof(int) + 255) & ~size_t(255)));
+  SplitResult* res = reinterpret_cast<SplitResult*>(reinterpret_cast<unsigned char*>(ctl) + 256);
+
+  if (wide) {
+    SM_CUDA_CHECK(cudaMemcpy2DAsync(Wx, sizeof(T) * ld, A, sizeof(T) * n, sizeof(T) * n, m,
+                                    cudaMemcpyDeviceToDevice, st));
+  } else {
+    SM_CHECK(transpose<T>(st, m, n, A, n, Wx, ld));
+  }
+  {
+    const size_t tot = (size_t)k * k;
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, 4096));
+    k_fill_rows<T><<<blocks, 256, 0, st>>>(k, l, Wx, ld);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+  }
+  SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
+  const double eps = DBL_EPSILON;
+  bool use_floor = false;
+  if (strat.method == SM_RELATIVE_NORM_SQUARED_ERROR)
+    use_floor = strat.tolerance >= 64.0 * k * (double)l * eps * eps;
+  else if (strat.method == SM_RELATIVE_SINGULAR_VALUE)
+    use_floor = strat.tolerance >= 16.0 * std::sqrt((double)k * l) * eps;
+  if (k >= 2) {
+    k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm0, 1);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    const double tol = std::sqrt((double)l) * DBL_EPSILON;
+    SM_CHECK(run_jacobi_noalloc<T>(st, Wx, ld, k, l, tol * tol, use_floor ? 1 : 0, nrm, nrm0, ctl));
+  }
+  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  k_sort_truncate<<<1, 1024, sizeof(unsigned long long) * (size_t)k, st>>>(
+      nrm, k, strat, perm, s_sorted, errors, ctl, res);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  SplitResult h;
+  SM_CUDA_CHECK(cudaMemcpyAsync(&h, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  if (h.status & DEV_BARRIER_TIMEOUT) {
+    set_error("svd: grid barrier timed out");
+    return SM_ERR_TIMEOUT;
+  }
+  if (h.status & (DEV_NONFINITE | DEV_NOT_CONVERGED)) {
+    set_error("SVD did not converge");
+    return SM_ERR_LINALG;
+  }
+  const int D = h.D;
+  const size_t total = (size_t)m * D + (size_t)D * n;
+  const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+  k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(wide, m, n, D, Wx, ld, Wx + l, ld, perm, s_sorted,
+                                                 OUT_U, left, OUT_SVT, right);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  *D_out = D;
+  *err_out = std::sqrt(h.err2);
+  return SM_OK;
+}
+
 }  // namespace sm
+
+extern "C" int sm_left_orth_2site_noalloc(int dtype, const void* AA, int a, int d1, int d2, int b,
+                                          const sm_strategy* st, void* U, void* SV, int* D,
+                                          double* err, void* stream) {
+  using namespace sm;
+  if (!st || !AA || !U || !SV || !D || !err) {
+    set_error("sm_left_orth_2site_noalloc: null argument");
+    return SM_ERR_VALUE;
+  }
+  if (st->tolerance < 0 || st->tolerance >= 1.0 || st->max_bond_dimension <= 0 || st->method < 0 ||
+      st->method > 3) {
+    set_error("Invalid Strategy passed to sm_left_orth_2site_noalloc");
+    return SM_ERR_STRATEGY;
+  }
+  if (a <= 0 || d1 <= 0 || d2 <= 0 || b <= 0) {
+    set_error("sm_left_orth_2site_noalloc: non-positive dimension");
+    return SM_ERR_VALUE;
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (dtype == SM_FLOAT64)
+    return left_orth_2site_noalloc<double>(s, (const double*)AA, a * d1, d2 * b, *st, (double*)U,
+                                           (double*)SV, D, err);
+  if (dtype == SM_COMPLEX128)
+    return left_orth_2site_noalloc<cplx>(s, (const cplx*)AA, a * d1, d2 * b, *st, (cplx*)U,
+                                         (cplx*)SV, D, err);
+  set_error("dtype must be SM_FLOAT64 or SM_COMPLEX128");
+  return SM_ERR_VALUE;
+}
