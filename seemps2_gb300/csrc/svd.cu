@@ -38,7 +38,8 @@ struct JacobiCtl {
   unsigned int rot[2];
   int status;
   int sweeps;
-  int pad[2];
+  int nact;  // rows still taking part in the iteration (deflation)
+  int pad;
 };
 
 // Grid-wide barrier with a bounded spin: one arrival counter and a generation
@@ -182,28 +183,73 @@ template <> struct Rot<cplx> {
 // rotated against each other sweep after sweep.  The caller sets it only when
 // the truncation rule is certain to discard every such vector.
 template <typename T, int NT, int E>
-__global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, double tol2,
-                                               int use_floor, int max_sweeps, double* nrm,
-                                               const double* nrm0, JacobiCtl* ctl) {
+__global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, int L, double tol2,
+                                               int use_floor, double defl_rel, double defl_abs,
+                                               int max_sweeps, double* nrm, const double* nrm0,
+                                               int* act, JacobiCtl* ctl) {
   constexpr int NW = NT / 32;
   __shared__ double part[2][NW][4];
-  __shared__ int sflag;
+  __shared__ int sflag, snact;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int kp = k + (k & 1);
-  const int rounds = kp - 1, npairs = kp / 2;
-  const int L = l + k;
   volatile int* vflag = reinterpret_cast<volatile int*>(ctl->rot);
+  double frob2 = 0.0;  // |A|_F^2 from the squared row norms, fixed order
+  for (int i = lane; i < k; i += 32) frob2 += __ldcg(nrm0 + i);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) frob2 += __shfl_xor_sync(0xffffffffu, frob2, o);
   double tiny2 = 0.0;
   if (use_floor) {
-    double frob2 = 0.0;  // |A|_F^2 from the squared row norms, fixed order
-    for (int i = lane; i < k; i += 32) frob2 += __ldcg(nrm0 + i);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) frob2 += __shfl_xor_sync(0xffffffffu, frob2, o);
     const double tiny = 16.0 * l * DBL_EPSILON * DBL_EPSILON * frob2;
     tiny2 = tiny * tiny;
   }
+  // rows whose squared norm falls to thr or below are deflated: the
+  // truncation rule certainly discards them, so they leave the round-robin
+  const double thr = defl_abs > 0.0 ? fmin(defl_rel * frob2, defl_abs) : defl_rel * frob2;
   int it = 0;  // pair iterations of this CTA (selects the smem buffer)
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    // exact squared norms at the start of every sweep
+    for (int i = blockIdx.x; i < k; i += gridDim.x) {
+      double a = 0.0;
+      for (int x = tid; x < l; x += NT) a += S<T>::abs2(ldcg(Wx + (size_t)i * ld + x));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) part[0][warp][0] = a;
+      __syncthreads();
+      if (tid == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NW; ++w) s += part[0][w][0];
+        __stcg(nrm + i, s);
+      }
+      __syncthreads();
+    }
+    if (!grid_sync(ctl)) return;
+    // every CTA read the previous sweep's rotation flag before this barrier
+    if (sweep > 0 && blockIdx.x == 0 && tid == 0) vflag[(sweep + 1) & 1] = 0;
+    // active rows, in ascending order, compacted by CTA 0
+    if (blockIdx.x == 0) {
+      __shared__ int wcount[NW];
+      int base = 0;
+      for (int i0 = 0; i0 < k; i0 += NT) {
+        const int i = i0 + tid;
+        const bool on = i < k && __ldcg(nrm + i) > thr;
+        const unsigned int bal = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) wcount[warp] = __popc(bal);
+        __syncthreads();
+        int off = base;
+        for (int w = 0; w < warp; ++w) off += wcount[w];
+        if (on) act[off + __popc(bal & ((1u << lane) - 1u))] = i;
+        int tot = 0;
+        for (int w = 0; w < NW; ++w) tot += wcount[w];
+        base += tot;
+        __syncthreads();
+      }
+      if (tid == 0) ((volatile int*)&ctl->nact)[0] = base;
+    }
+    if (!grid_sync(ctl)) return;
+    if (tid == 0) snact = ((volatile int*)&ctl->nact)[0];
+    __syncthreads();
+    const int ka = snact;
+    const int kp = ka + (ka & 1);
+    const int rounds = ka >= 2 ? kp - 1 : 0, npairs = kp / 2;
     for (int r = 0; r < rounds; ++r) {
       for (int t = blockIdx.x; t < npairs; t += gridDim.x, ++it) {
         int p, q;
@@ -215,25 +261,9 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, doub
           q = (r + kp - 1 - t) % (kp - 1);
         }
         double (*pt)[4] = part[it & 1];
-        if (p >= k || q >= k) {
-          // the dummy player of an odd k: its partner idles this round, but
-          // in the first round its exact squared norm must still be refreshed
-          if (r == 0) {
-            const int row = p < q ? p : q;
-            double a = 0.0;
-            for (int x = tid; x < l; x += NT) a += S<T>::abs2(ldcg(Wx + (size_t)row * ld + x));
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-            if (lane == 0) pt[warp][0] = a;
-            __syncthreads();
-            if (tid == 0) {
-              double s = 0.0;
-              for (int w = 0; w < NW; ++w) s += pt[w][0];
-              __stcg(nrm + row, s);
-            }
-          }
-          continue;
-        }
+        if (p >= ka || q >= ka) continue;  // the dummy player of an odd count
+        p = __ldcg(act + p);
+        q = __ldcg(act + q);
         if (p > q) { const int tmp = p; p = q; q = tmp; }
         T* rp = Wx + (size_t)p * ld;
         T* rq = Wx + (size_t)q * ld;
@@ -256,10 +286,6 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, doub
           for (int e = 0; e < E; ++e) {
             const int x = tid + NT * e;
             if (x < l) {
-              if (r == 0) {
-                a += S<T>::abs2(u[e]);
-                b += S<T>::abs2(v[e]);
-              }
               if (e & 1) g1 = S<T>::cfma(u[e], v[e], g1);
               else g0 = S<T>::cfma(u[e], v[e], g0);
             }
@@ -267,78 +293,106 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, doub
         } else {
           for (int x = tid; x < l; x += NT) {
             const T uu = ldcg(rp + x), vv = ldcg(rq + x);
-            if (r == 0) {
-              a += S<T>::abs2(uu);
-              b += S<T>::abs2(vv);
-            }
             g0 = S<T>::cfma(uu, vv, g0);
           }
         }
+        constexpr bool kCplx = sizeof(T) != sizeof(double);
         double gr, gi, hr, hi;
         gamma_parts(g0, gr, gi);
         gamma_parts(g1, hr, hi);
         gr += hr;
-        gi += hi;
+        if constexpr (kCplx) gi += hi;
+        // every reduced value costs one FP64 add per level (each FP64 warp
+        // instruction occupies a sub-partition's FP64 pipe for ~64 cycles on
+        // GB300), so only the values this round needs are reduced
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
           gr += __shfl_xor_sync(0xffffffffu, gr, o);
-          gi += __shfl_xor_sync(0xffffffffu, gi, o);
-          if (r == 0) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            b += __shfl_xor_sync(0xffffffffu, b, o);
-          }
+          if constexpr (kCplx) gi += __shfl_xor_sync(0xffffffffu, gi, o);
         }
         if (lane == 0) {
           pt[warp][0] = gr;
           pt[warp][1] = gi;
-          pt[warp][2] = a;
-          pt[warp][3] = b;
         }
         __syncthreads();
-        gr = gi = 0.0;
-        if (r == 0) a = b = 0.0;
+        gr = pt[0][0];
+        if constexpr (kCplx) gi = pt[0][1];
 #pragma unroll
-        for (int w = 0; w < NW; ++w) {  // same order in every thread
+        for (int w = 1; w < NW; ++w) {  // same order in every thread
           gr += pt[w][0];
-          gi += pt[w][1];
-          if (r == 0) {
-            a += pt[w][2];
-            b += pt[w][3];
-          }
+          if constexpr (kCplx) gi += pt[w][1];
         }
-        if (r != 0) {
-          a = __ldcg(nrm + p);
-          b = __ldcg(nrm + q);
-        }
-        const double g2 = gr * gr + gi * gi;
+        if constexpr (!kCplx) gi = 0.0;
+        // squared norms: exact at the start of the sweep, updated in closed
+        // form after each rotation
+        a = __ldcg(nrm + p);
+        b = __ldcg(nrm + q);
+        const double g2 = kCplx ? fma(gr, gr, gi * gi) : gr * gr;
         const bool rot = g2 > tiny2 && g2 > tol2 * a * b;
         double na = a, nb = b;
         if (rot) {
-          const double rsq = rsqrt(g2);  // 1/|g|
-          const double zeta = 0.5 * (b - a) * rsq;
-          double tt;
-          if (fabs(zeta) < 1e18) {
-            const float zf = (float)zeta;
+          // Angle in FP32 on values scaled by a power of two so that a + b
+          // lands in [1, 2): zeta = (b - a) / 2|g|, t = sign(zeta) /
+          // (|zeta| + sqrt(1 + zeta^2)).  The (c, s) pair (and the complex
+          // phase) are then brought to unit norm in FP64 with a two-term
+          // correction f = 1 - d/2 + 3d^2/8, d = c^2 + s^2 - 1 ~ 1e-7, which
+          // leaves c^2 + s^2 - 1 = O(d^3): each rotation is unitary to FP64
+          // rounding whatever the accuracy of the angle.
+          const int ex = (__double2hiint(a + b) >> 20) & 0x7ff;
+          const double sc = __hiloint2double((2046 - ex) << 20, 0);     // 2^(1023 - ex)
+          const double sc_inv = __hiloint2double(ex << 20, 0);           // 2^(ex - 1023)
+          const float as = (float)(a * sc), bs = (float)(b * sc);
+          const float grs = (float)(gr * sc), gis = kCplx ? (float)(gi * sc) : 0.0f;
+          const float gabs_f = kCplx ? sqrtf(fmaf(grs, grs, gis * gis)) : fabsf(grs);
+          double tt, c, sn;
+          float zf = 0.0f;
+          const bool fp32_ok = ex > 0 && ex < 2046 && gabs_f > 1e-30f;
+          if (fp32_ok) zf = 0.5f * (bs - as) / gabs_f;
+          if (fp32_ok && fabsf(zf) < 1e18f) {
             const float az = fabsf(zf);
-            tt = (double)copysignf(1.0f / (az + sqrtf(fmaf(az, az, 1.0f))), zf);
+            const float tf = copysignf(1.0f / (az + sqrtf(fmaf(az, az, 1.0f))), zf);
+            const float cf = rsqrtf(fmaf(tf, tf, 1.0f));
+            const double c64 = (double)cf, s64 = (double)(cf * tf);
+            const double d = fma(c64, c64, fma(s64, s64, -1.0));
+            const double f = fma(d, fma(0.375, d, -0.5), 1.0);
+            c = c64 * f;
+            sn = s64 * f;
+            tt = (double)tf;
           } else {
-            tt = __drcp_rn(2.0 * zeta);
+            // extremely graded pair (|g| below 1e-30 (a + b) or |zeta| >= 1e18):
+            // the whole angle in FP64, rare
+            const double zeta = 0.5 * (b - a) / sqrt(g2);
+            const double az = fabs(zeta);
+            tt = az < 1e150 ? 1.0 / (az + sqrt(fma(az, az, 1.0))) : 0.5 / az;
+            tt = copysign(tt, zeta);
+            c = 1.0 / sqrt(fma(tt, tt, 1.0));
+            sn = c * tt;
           }
-          const double c = rsqrt(fma(tt, tt, 1.0));
-          const double sn = c * tt;
           double er, ei;
-          if constexpr (sizeof(T) == sizeof(double)) {
+          if constexpr (kCplx) {
+            if (fp32_ok) {
+              const float inv = 1.0f / gabs_f;
+              const double e_r = (double)(grs * inv), e_i = (double)(gis * inv);
+              const double de = fma(e_r, e_r, fma(e_i, e_i, -1.0));
+              const double fe = fma(de, fma(0.375, de, -0.5), 1.0);
+              er = e_r * fe;
+              ei = e_i * fe;
+            } else {
+              const double inv = 1.0 / sqrt(g2);
+              er = gr * inv;
+              ei = gi * inv;
+            }
+          } else {
             er = gr >= 0.0 ? 1.0 : -1.0;  // the phase of a real overlap is its sign
             ei = 0.0;
-          } else {
-            er = gr * rsq;
-            ei = gi * rsq;
           }
+          // closed-form norm update (approximate; exact norms return at the
+          // first round of the next sweep)
+          const double gabs = fp32_ok ? (double)gabs_f * sc_inv : sqrt(g2);
+          na = fma(-tt, gabs, a);
+          nb = fma(tt, gabs, b);
           Rot<T> R;
           R.set(c, sn, er, ei);
-          const double cs2 = 2.0 * c * sn * (g2 * rsq);
-          na = fma(c * c, a, fma(sn * sn, b, -cs2));
-          nb = fma(sn * sn, a, fma(c * c, b, cs2));
           if constexpr (E > 0) {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
@@ -359,14 +413,12 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, doub
           }
           if (tid == 0) vflag[sweep & 1] = 1;
         }
-        if (tid == 0 && (rot || r == 0)) {
+        if (tid == 0 && rot) {
           __stcg(nrm + p, na);
           __stcg(nrm + q, nb);
         }
       }
       if (!grid_sync(ctl)) return;
-      // slot (sweep+1)&1 was read by every CTA before this barrier: recycle it
-      if (r == 0 && sweep > 0 && blockIdx.x == 0 && tid == 0) vflag[(sweep + 1) & 1] = 0;
     }
     if (tid == 0) sflag = vflag[sweep & 1];
     __syncthreads();
@@ -534,9 +586,32 @@ constexpr int kMaxSweeps = 60;
 
 constexpr int kJacobiNT = 128;
 
+// Deflation thresholds on a row's squared norm, relative to |A|_F^2 (rel) or
+// absolute (abs), below which the strategy certainly discards the row's
+// singular value: the relative-norm rule drops a tail of total weight up to
+// tol |A|_F^2, so rows of at most 1e-6 tol |A|_F^2 / k each are dropped even
+// all together; the singular-value rules drop s <= tol s_max (or <= tol), and
+// |A|_F^2 <= k s_max^2.  No deflation without truncation or at tol = 0.
+static void deflation(const sm_strategy& s, int k, double* rel, double* abs_) {
+  // A deflated row keeps a singular value of at most sqrt(rel k) s_max that
+  // the iteration no longer refines, so rel <= 1e-24 / k also bounds its
+  // error by 1e-12 s_max.
+  *rel = 0.0;
+  *abs_ = 0.0;
+  if (s.tolerance <= 0.0) return;
+  if (s.method == SM_RELATIVE_NORM_SQUARED_ERROR) *rel = std::min(1e-24, 1e-6 * s.tolerance) / k;
+  else if (s.method == SM_RELATIVE_SINGULAR_VALUE)
+    *rel = std::min(1e-24, 1e-4 * s.tolerance * s.tolerance) / k;
+  else if (s.method == SM_ABSOLUTE_SINGULAR_VALUE) {
+    *rel = 1e-24 / k;
+    *abs_ = 1e-4 * s.tolerance * s.tolerance;
+  }
+}
+
 template <typename T, int E>
-int launch_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double tol2,
-                  int use_floor, double* nrm, const double* nrm0, JacobiCtl* ctl) {
+int launch_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, int L, double tol2,
+                  int use_floor, double defl_rel, double defl_abs, double* nrm, const double* nrm0,
+                  int* act, JacobiCtl* ctl) {
   const int npairs = (k + (k & 1)) / 2;
   const int sms = std::max(1, ctx.num_sms);
   auto fn = k_jacobi<T, kJacobiNT, E>;
@@ -552,18 +627,24 @@ int launch_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double
   }
   const int grid = std::max(1, std::min(npairs, per_sm * sms));
   int ms = kMaxSweeps;
-  void* args[] = {&Wx, &ld, &k, &l, &tol2, &use_floor, &ms, &nrm, &nrm0, &ctl};
+  void* args[] = {&Wx, &ld, &k, &l, &L, &tol2, &use_floor, &defl_rel, &defl_abs, &ms, &nrm,
+                  &nrm0, &act, &ctl};
   SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
                                             dim3(kJacobiNT), args, 0, st));
   note_launch();
   return SM_OK;
 }
 
+// Rows of length L: l entries of the vector, then (L - l) accumulated-unitary
+// entries (L = l + k when the short-side factor is accumulated, L = l when not).
 template <typename T>
-int run_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
-               double* nrm, const double* nrm0, JacobiCtl* ctl) {
-  const int need = (l + k + kJacobiNT - 1) / kJacobiNT;
-#define SM_J(EV) return launch_jacobi<T, EV>(ctx, st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl)
+int run_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, int L, double tol2,
+               int use_floor, double defl_rel, double defl_abs, double* nrm, const double* nrm0,
+               int* act, JacobiCtl* ctl) {
+  const int need = (L + kJacobiNT - 1) / kJacobiNT;
+#define SM_J(EV)                                                                              \
+  return launch_jacobi<T, EV>(ctx, st, Wx, ld, k, l, L, tol2, use_floor, defl_rel, defl_abs, nrm, \
+                              nrm0, act, ctl)
   if constexpr (sizeof(T) == sizeof(double)) {
     if (need <= 1) SM_J(1);
     if (need <= 2) SM_J(2);
@@ -614,6 +695,359 @@ int truncate_device(Ctx& ctx, cudaStream_t st, const double* s_dev, int n,
   return SM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Rank-revealing Householder QR preconditioner (FP64, no pivoting).
+//
+// The one-sided Jacobi iteration on the rows of W (k x l) is replaced by the
+// same iteration on the rows of R from W = Q R: both have the same singular
+// values and right singular vectors, but the rows of R converge in fewer
+// sweeps, and for a numerically rank-deficient W (a two-site tensor of rank
+// ~chi inside a 2chi x 2chi matrix) the trailing rows of R are already at
+// rounding level, so the Jacobi deflation drops them before the first sweep.
+// The factorisation stops early once the trailing block holds at most `thr`
+// of |W|_F^2, the weight the truncation rule certainly discards.
+//
+// Storage: Wt = W^T (l x k, row-major) so that every column of W is a
+// contiguous row; one warp owns a column.  Step j applies the reflector
+// H_j = I - tau v v^H (published in the previous step, double-buffered by
+// step parity) to every column c > j; the warp owning column j + 1 then forms
+// the next reflector.  One bounded grid barrier per step.
+// ---------------------------------------------------------------------------
+struct QrCtl {
+  JacobiCtl bar;  // barrier words and status, shared layout with the Jacobi kernel
+  int steps;      // reflections performed (the rank estimate)
+  int pad;
+  double tau[2];  // tau of the published reflector, by step parity
+};
+
+__device__ bool qr_grid_sync(QrCtl* ctl) { return grid_sync(&ctl->bar); }
+
+// Reflector for x = Wt[c][j:k]: v = x + nu e1, nu = (x0/|x0|) |x|,
+// tau = 1 / (|x| (|x| + |x0|)); writes v (v0 = x0 + nu) to vdst[j:k] and sets
+// Wt[c][j] = -nu, the diagonal of R.  Executed by one warp.
+template <typename T>
+__device__ void qr_reflector(T* row, int j, int k, T* vdst, double* tau_out) {
+  const int lane = threadIdx.x & 31;
+  double nx2 = 0.0;
+  for (int i = j + lane; i < k; i += 32) nx2 += S<T>::abs2(ldcg(row + i));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nx2 += __shfl_xor_sync(0xffffffffu, nx2, o);
+  const T x0 = ldcg(row + j);
+  const double nx = sqrt(nx2);
+  const double a0 = sqrt(S<T>::abs2(x0));
+  T nu;
+  if (a0 > 0.0) nu = S<T>::scale(x0, nx / a0);
+  else nu = S<T>::scale(S<T>::one(), nx);
+  const double tau = nx > 0.0 ? 1.0 / (nx * (nx + a0)) : 0.0;
+  for (int i = j + lane; i < k; i += 32) {
+    T v = ldcg(row + i);
+    if (i == j) v = v + nu;
+    stcg(vdst + i, v);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    stcg(row + j, S<T>::scale(nu, -1.0));
+    *tau_out = tau;
+  }
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_house_qr(T* Wt, int k, int l, double thr_rel,
+                                                 T* vbuf, double* part, QrCtl* ctl) {
+  constexpr int NW = NT / 32;
+  __shared__ double wpart[NW];
+  __shared__ int stop_flag;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * NW + warp, nw = gridDim.x * NW;
+  const int nmax = k < l ? k : l;
+  // |W|_F^2
+  {
+    double a = 0.0;
+    for (int c = gw; c < l; c += nw)
+      for (int i = lane; i < k; i += 32) a += S<T>::abs2(ldcg(Wt + (size_t)c * k + i));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) wpart[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < NW; ++w) t += wpart[w];
+      __stcg(part + blockIdx.x, t);
+    }
+    // reflector 0 from column 0
+    if (gw == 0) qr_reflector<T>(Wt, 0, k, vbuf, &ctl->tau[0]);
+  }
+  if (!qr_grid_sync(ctl)) return;
+  // per-CTA partials summed by every warp in the same order (lane-strided,
+  // then a fixed shuffle tree): a serial FP64 sum over 100+ CTAs costs
+  // microseconds on GB300's FP64 unit
+  double frob2 = 0.0;
+  for (int b = lane; b < (int)gridDim.x; b += 32) frob2 += __ldcg(part + b);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) frob2 += __shfl_xor_sync(0xffffffffu, frob2, o);
+  const double thr = thr_rel * frob2;
+  int steps = nmax;
+  for (int j = 0; j < nmax; ++j) {
+    const T* v = vbuf + (size_t)(j & 1) * k;
+    const double tau = ((volatile double*)ctl->tau)[j & 1];
+    double trail = 0.0;
+    for (int c = gw; c < l; c += nw) {
+      if (c <= j) continue;
+      T* row = Wt + (size_t)c * k;
+      T w = S<T>::zero();
+      for (int i = j + lane; i < k; i += 32) w = S<T>::cfma(ldcg(v + i), ldcg(row + i), w);
+      double wr, wi;
+      gamma_parts(w, wr, wi);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        wr += __shfl_xor_sync(0xffffffffu, wr, o);
+        wi += __shfl_xor_sync(0xffffffffu, wi, o);
+      }
+      T tw;
+      if constexpr (sizeof(T) == sizeof(double)) tw = tau * wr;
+      else tw = cplx{tau * wr, tau * wi};
+      for (int i = j + lane; i < k; i += 32) {
+        // y -= tau (v^H y) v
+        T y = ldcg(row + i);
+        const T vi = ldcg(v + i);
+        y = y - tw * vi;
+        stcg(row + i, y);
+        if (i > j) trail += S<T>::abs2(y);
+      }
+      if (c == j + 1 && j + 1 < nmax) {
+        // this column's entries below row j were counted in the trailing
+        // block above, before the next reflection moves them into R
+        __syncwarp();
+        qr_reflector<T>(row, j + 1, k, vbuf + (size_t)((j + 1) & 1) * k, &ctl->tau[(j + 1) & 1]);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) trail += __shfl_xor_sync(0xffffffffu, trail, o);
+    if (lane == 0) wpart[warp] = trail;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < NW; ++w) t += wpart[w];
+      __stcg(part + blockIdx.x, t);
+    }
+    if (!qr_grid_sync(ctl)) return;
+    if (warp == 0) {
+      double tot = 0.0;
+      for (int b = lane; b < (int)gridDim.x; b += 32) tot += __ldcg(part + b);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+      if (lane == 0) stop_flag = tot <= thr;
+    }
+    __syncthreads();
+    if (stop_flag) {
+      steps = j + 1;
+      break;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->steps = steps;
+}
+
+// Wx[i][c] = R[i][c] from Wt after `steps` reflections: row i < steps is the
+// upper-triangular row of R; rows i >= steps are the trailing block rows.
+template <typename T>
+__global__ void k_qr_extract(const T* __restrict__ Wt, int k, int l, int kk, const QrCtl* ctl,
+                             T* __restrict__ Wx, JacobiCtl* jctl) {
+  const int steps = ctl->steps;
+  // a QR barrier timeout is reported through the Jacobi status word
+  if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->bar.status)
+    atomicOr(&jctl->status, ctl->bar.status);
+  const size_t total = (size_t)kk * l;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / l), c = (int)(e % l);
+    const int first = i < steps ? i : steps;
+    Wx[e] = c >= first ? Wt[(size_t)c * k + i] : S<T>::zero();
+  }
+}
+
+// Split where only one factor must be an isometry: U for (OUT_U, OUT_SVT)
+// (left_orth_2site, right canonical update) and V for (OUT_US, OUT_VT).
+// The Jacobi iteration then orthogonalises the vectors of that side -- the
+// columns of A (rows of A^T) for U, the rows of A for V -- without
+// accumulating a unitary: after convergence those vectors are s_i times the
+// singular vectors, so the isometry is the normalised rows and the other
+// factor is one FP64 GEMM, S V = U^H A or U S = A V^H.  Used when the
+// orthogonalised side is also the short side (k = min(m, n)), which keeps
+// the singular-value count and the truncation input identical to the full
+// SVD's.
+template <typename T>
+int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
+                    bool want_u, T* left, T* right, double* s_out, SplitResult* out) {
+  // W (kw x l): its rows are orthogonalised -- W = A^T for U, W = A for V
+  const int kw = want_u ? n : m;
+  const int l = want_u ? m : n;
+  const int k = std::min(kw, l);  // rows of R, = min(m, n) singular values
+  const int ld = l;
+  T *Wt, *Wx, *vbuf;
+  double *nrm, *nrm0, *s_sorted, *errors, *qpart;
+  int *perm, *act;
+  JacobiCtl* ctl;
+  QrCtl* qctl;
+  SplitResult* res;
+  SM_CHECK(ctx.scratch("svd.Wt", (size_t)l * kw, &Wt));
+  SM_CHECK(ctx.scratch("svd.Wx", (size_t)k * ld, &Wx));
+  SM_CHECK(ctx.scratch("svd.v", (size_t)2 * kw, &vbuf));
+  SM_CHECK(ctx.scratch("svd.nrm", (size_t)k, &nrm));
+  SM_CHECK(ctx.scratch("svd.nrm0", (size_t)k, &nrm0));
+  SM_CHECK(ctx.scratch("svd.s", (size_t)k, &s_sorted));
+  SM_CHECK(ctx.scratch("svd.err", (size_t)k + 1, &errors));
+  SM_CHECK(ctx.scratch("svd.perm", (size_t)k, &perm));
+  SM_CHECK(ctx.scratch("svd.act", (size_t)k, &act));
+  SM_CHECK(ctx.scratch("svd.ctl", 1, &ctl));
+  SM_CHECK(ctx.scratch("svd.qctl", 1, &qctl));
+  SM_CHECK(ctx.scratch("svd.res", 1, &res));
+  // Wt = W^T (l x kw): A itself for U, A^T for V
+  if (want_u) {
+    SM_CUDA_CHECK(cudaMemcpyAsync(Wt, A, sizeof(T) * (size_t)m * n, cudaMemcpyDeviceToDevice, st));
+  } else {
+    SM_CHECK(transpose<T>(st, m, n, A, n, Wt, m));
+  }
+  double drel, dabs;
+  deflation(strat, k, &drel, &dabs);
+  // rank-revealing QR preconditioner: W = Q R, R has k rows
+  {
+    constexpr int QNT = 128;
+    auto fn = k_house_qr<T, QNT>;
+    const void* key = reinterpret_cast<const void*>(fn);
+    int per_sm = 0;
+    const auto it = ctx.coop_blocks.find(key);
+    if (it != ctx.coop_blocks.end()) per_sm = it->second;
+    else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, QNT, 0) != cudaSuccess) per_sm = 1;
+      per_sm = std::max(1, per_sm);
+      ctx.coop_blocks[key] = per_sm;
+    }
+    const int grid = std::max(1, std::min((l + QNT / 32 - 1) / (QNT / 32), per_sm * std::max(1, ctx.num_sms)));
+    SM_CHECK(ctx.scratch("svd.qpart", (size_t)grid, &qpart));
+    SM_CUDA_CHECK(cudaMemsetAsync(qctl, 0, sizeof(QrCtl), st));
+    int kk = kw, ll = l;
+    void* args[] = {&Wt, &kk, &ll, &drel, &vbuf, &qpart, &qctl};
+    SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
+                                              dim3(QNT), args, 0, st));
+    note_launch();
+    const size_t tot = (size_t)k * l;
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, 4096));
+    SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
+    k_qr_extract<T><<<blocks, 256, 0, st>>>(Wt, kw, l, k, qctl, Wx, ctl);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+  }
+  const double eps = DBL_EPSILON;
+  bool use_floor = false;
+  if (strat.method == SM_RELATIVE_NORM_SQUARED_ERROR)
+    use_floor = strat.tolerance >= 64.0 * k * (double)l * eps * eps;
+  else if (strat.method == SM_RELATIVE_SINGULAR_VALUE)
+    use_floor = strat.tolerance >= 16.0 * std::sqrt((double)k * l) * eps;
+  if (k >= 2) {
+    k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm0, 1);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    const double tol = std::sqrt((double)l) * DBL_EPSILON;
+    if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+    SM_CHECK(run_jacobi<T>(ctx, st, Wx, ld, k, l, l, tol * tol, use_floor ? 1 : 0, drel, dabs, nrm,
+                           nrm0, act, ctl));
+    if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+    ctx.stats.jacobi_launches += 1;
+    ctx.stats.jacobi_flops += (4.0 * std::max(m, n) * (double)k * k + 8.0 * (double)k * k * k) *
+                              (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
+  }
+  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  const size_t smem = sizeof(unsigned long long) * (size_t)k;
+  if (smem > 200 * 1024) {
+    set_error("svd: matrix too large for the on-chip sort");
+    return SM_ERR_VALUE;
+  }
+  if (smem > 48 * 1024)
+    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+  k_sort_truncate<<<1, 1024, smem, st>>>(nrm, k, strat, perm, s_sorted, errors, ctl, res);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  SplitResult* h = reinterpret_cast<SplitResult*>(ctx.pinned);
+  SM_CUDA_CHECK(cudaMemcpyAsync(h, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  *out = *h;
+  ctx.stats.splits += 1;
+  ctx.stats.jacobi_sweeps += h->sweeps;
+  if (ctx.timing && k >= 2) {
+    float ms = 0.f;
+    SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+    ctx.stats.jacobi_ms += ms;
+  }
+  if (h->status & DEV_BARRIER_TIMEOUT) {
+    set_error("svd: grid barrier timed out");
+    return SM_ERR_TIMEOUT;
+  }
+  if (h->status & DEV_NONFINITE) {
+    set_error("SVD did not converge (non-finite values)");
+    return SM_ERR_LINALG;
+  }
+  if (h->status & DEV_NOT_CONVERGED) {
+    set_error("SVD did not converge");
+    return SM_ERR_LINALG;
+  }
+  if (s_out)
+    SM_CUDA_CHECK(cudaMemcpyAsync(s_out, s_sorted, sizeof(double) * k, cudaMemcpyDeviceToDevice, st));
+  if (ctx.trace) {
+    const size_t off = ctx.tr_s.size();
+    ctx.tr_s.resize(off + k);
+    SM_CUDA_CHECK(cudaMemcpyAsync(ctx.tr_s.data() + off, s_sorted, sizeof(double) * k,
+                                  cudaMemcpyDeviceToHost, st));
+    SM_CUDA_CHECK(cudaStreamSynchronize(st));
+    ctx.tr_rank.push_back(h->D);
+    ctx.tr_len.push_back(k);
+    ctx.tr_err2.push_back(h->err2);
+  }
+  const int D = h->D;
+  const T one = S<T>::one(), zero = S<T>::zero();
+  // The closing GEMM reads A: when an output buffer overlaps A (the canonical
+  // updates write the new site over the old one), stage both outputs.
+  const char* a0 = reinterpret_cast<const char*>(A);
+  const char* a1 = a0 + sizeof(T) * (size_t)m * n;
+  auto overlaps = [&](const T* p, size_t count) {
+    const char* p0 = reinterpret_cast<const char*>(p);
+    return p0 < a1 && p0 + sizeof(T) * count > a0;
+  };
+  const size_t n_iso = want_u ? (size_t)m * D : (size_t)D * n;
+  const size_t n_oth = want_u ? (size_t)D * n : (size_t)m * D;
+  T* iso = want_u ? left : right;
+  T* oth = want_u ? right : left;
+  const bool stage = overlaps(iso, n_iso) || overlaps(oth, n_oth);
+  T *iso_w = iso, *oth_w = oth;
+  if (stage) {
+    SM_CHECK(ctx.scratch("svd.iso", n_iso, &iso_w));
+    SM_CHECK(ctx.scratch("svd.oth", n_oth, &oth_w));
+  }
+  const int blocks = (int)std::min<size_t>((n_iso + 255) / 256, 4096);
+  if (want_u) {
+    // U (m x D) = normalised rows of W^T; then S V (D x n) = U^H A
+    k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(0, m, n, D, Wx, ld, Wx, ld, perm, s_sorted, OUT_U,
+                                                   iso_w, 0, oth_w);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, D, n, m, one, iso_w, D, A, n, zero, oth_w, n));
+  } else {
+    // V (D x n) = normalised rows of W; then U S (m x D) = A V^H
+    k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(1, m, n, D, Wx, ld, Wx, ld, perm, s_sorted, 0,
+                                                   oth_w, OUT_VT, iso_w);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, m, D, n, one, A, n, iso_w, n, zero, oth_w, D));
+  }
+  if (stage) {
+    SM_CUDA_CHECK(cudaMemcpyAsync(iso, iso_w, sizeof(T) * n_iso, cudaMemcpyDeviceToDevice, st));
+    SM_CUDA_CHECK(cudaMemcpyAsync(oth, oth_w, sizeof(T) * n_oth, cudaMemcpyDeviceToDevice, st));
+  }
+  return SM_OK;
+}
+
 template <typename T>
 int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
               int left_mode, T* left, int right_mode, T* right, double* s_out,
@@ -622,6 +1056,10 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     set_error("svd: empty matrix");
     return SM_ERR_VALUE;
   }
+  if (left_mode == OUT_U && right_mode == OUT_SVT)
+    return svd_split_xfree<T>(ctx, st, A, m, n, strat, true, left, right, s_out, out);
+  if (left_mode == OUT_US && right_mode == OUT_VT)
+    return svd_split_xfree<T>(ctx, st, A, m, n, strat, false, left, right, s_out, out);
   const int k = std::min(m, n), l = std::max(m, n);
   const bool wide = m <= n;
   const int ld = l + k;  // rows are [w (l) | x (k)]
@@ -671,7 +1109,12 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     SM_CUDA_CHECK(cudaGetLastError());
     const double tol = std::sqrt((double)l) * DBL_EPSILON;
     if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
-    SM_CHECK(run_jacobi<T>(ctx, st, Wx, ld, k, l, tol * tol, use_floor ? 1 : 0, nrm, nrm0, ctl));
+    double drel, dabs;
+    deflation(strat, k, &drel, &dabs);
+    int* act;
+    SM_CHECK(ctx.scratch("svd.act", (size_t)k, &act));
+    SM_CHECK(run_jacobi<T>(ctx, st, Wx, ld, k, l, l + k, tol * tol, use_floor ? 1 : 0, drel, dabs,
+                           nrm, nrm0, act, ctl));
     if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
     ctx.stats.jacobi_launches += 1;
     // 4 m n^2 + 8 n^3 with m >= n (x4 for complex arithmetic)
@@ -795,7 +1238,8 @@ static int noalloc_scratch(unsigned char** out) {
 // keeps occupancy results in a map; this one queries the runtime each time).
 template <typename T, int E>
 int launch_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
-                          double* nrm, const double* nrm0, JacobiCtl* ctl) {
+                          double defl_rel, double defl_abs, double* nrm, const double* nrm0,
+                          int* act, JacobiCtl* ctl) {
   const int npairs = (k + (k & 1)) / 2;
   int dev = 0, sms = 1, per_sm = 1;
   SM_CUDA_CHECK(cudaGetDevice(&dev));
@@ -804,7 +1248,9 @@ int launch_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double t
   SM_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kJacobiNT, 0));
   const int grid = std::max(1, std::min(npairs, std::max(1, per_sm) * std::max(1, sms)));
   int ms = kMaxSweeps;
-  void* args[] = {&Wx, &ld, &k, &l, &tol2, &use_floor, &ms, &nrm, &nrm0, &ctl};
+  int L = l + k;
+  void* args[] = {&Wx, &ld, &k, &l, &L, &tol2, &use_floor, &defl_rel, &defl_abs, &ms, &nrm,
+                  &nrm0, &act, &ctl};
   SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
                                             dim3(kJacobiNT), args, 0, st));
   note_launch();
@@ -813,14 +1259,18 @@ int launch_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double t
 
 template <typename T>
 int run_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
-                       double* nrm, const double* nrm0, JacobiCtl* ctl) {
+                       double defl_rel, double defl_abs, double* nrm, const double* nrm0, int* act,
+                       JacobiCtl* ctl) {
   // k <= 256 and l <= 256 here, so a thread holds at most 4 elements per row
   const int need = (l + k + kJacobiNT - 1) / kJacobiNT;
   if (need <= 1)
-    return launch_jacobi_noalloc<T, 1>(st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl);
+    return launch_jacobi_noalloc<T, 1>(st, Wx, ld, k, l, tol2, use_floor, defl_rel, defl_abs, nrm,
+                                       nrm0, act, ctl);
   if (need <= 2)
-    return launch_jacobi_noalloc<T, 2>(st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl);
-  return launch_jacobi_noalloc<T, 4>(st, Wx, ld, k, l, tol2, use_floor, nrm, nrm0, ctl);
+    return launch_jacobi_noalloc<T, 2>(st, Wx, ld, k, l, tol2, use_floor, defl_rel, defl_abs, nrm,
+                                       nrm0, act, ctl);
+  return launch_jacobi_noalloc<T, 4>(st, Wx, ld, k, l, tol2, use_floor, defl_rel, defl_abs, nrm,
+                                     nrm0, act, ctl);
 }
 
 template <typename T>
@@ -851,6 +1301,7 @@ int left_orth_2site_noalloc(cudaStream_t st, const T* A, int m, int n, const sm_
   JacobiCtl* ctl = reinterpret_cast<JacobiCtl*>(
       reinterpret_cast<unsigned char*>(perm) + ((kNoAllocMaxDim * sizeof(int) + 255) & ~size_t(255)));
   SplitResult* res = reinterpret_cast<SplitResult*>(reinterpret_cast<unsigned char*>(ctl) + 256);
+  int* act = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(res) + 256);
 
   if (wide) {
     SM_CUDA_CHECK(cudaMemcpy2DAsync(Wx, sizeof(T) * ld, A, sizeof(T) * n, sizeof(T) * n, m,
@@ -877,7 +1328,10 @@ int left_orth_2site_noalloc(cudaStream_t st, const T* A, int m, int n, const sm_
     note_launch();
     SM_CUDA_CHECK(cudaGetLastError());
     const double tol = std::sqrt((double)l) * DBL_EPSILON;
-    SM_CHECK(run_jacobi_noalloc<T>(st, Wx, ld, k, l, tol * tol, use_floor ? 1 : 0, nrm, nrm0, ctl));
+    double drel, dabs;
+    deflation(strat, k, &drel, &dabs);
+    SM_CHECK(run_jacobi_noalloc<T>(st, Wx, ld, k, l, tol * tol, use_floor ? 1 : 0, drel, dabs, nrm,
+                                   nrm0, act, ctl));
   }
   k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
   note_launch();
