@@ -154,14 +154,15 @@ def fp64_peak(torch, lib_mod) -> float:
     return best
 
 
-def cpu_run(mps, mpo, chi, sweeps=2):
-    """One oracle call (all host BLAS threads); returns (seconds, sweeps run)."""
+def cpu_run(mps, mpo, chi, sweeps=2, want_result=False):
+    """One oracle call (all host BLAS threads); returns (seconds, sweeps run[, result])."""
     from oracle import seemps_oracle as so
 
     st = so.DEFAULT_STRATEGY.replace(**strategy_kwargs(chi, sweeps))
     t = time.perf_counter()
     res = so.mpo_apply(mpo, mps, st)
-    return time.perf_counter() - t, res.sweeps
+    dt = time.perf_counter() - t
+    return (dt, res.sweeps, res) if want_result else (dt, res.sweeps)
 
 
 def run_reference(args):
@@ -203,6 +204,51 @@ def workload_config(args):
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
 
+def run_split_case(args):
+    """Single two-site splits (left-orthogonal, as in a left-to-right sweep) of an
+    M x N matrix whose spectrum has the shape of the n=30, chi=256 workload's
+    splits (256 values from 1 to 3e-3, two more at 2.5e-3 and 2.4e-3, then
+    zeros), timed with CUDA events for both precision modes."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import seemps2_gb300 as sg
+    from seemps2_gb300 import _lib, core
+
+    m, n = args.split_case
+    rng = np.random.default_rng(SEED)
+    k = min(m, n)
+    s = np.concatenate([np.geomspace(1.0, 3e-3, 256), [2.5e-3, 2.4e-3]])[:k]
+    Qa, _ = np.linalg.qr(rng.normal(size=(m, len(s))))
+    Qb, _ = np.linalg.qr(rng.normal(size=(n, len(s))))
+    A = (Qa * s) @ Qb.T
+    AA = torch.from_numpy(np.ascontiguousarray(A.reshape(m // 2, 2, 2, n // 2))).cuda()
+    st = sg.Strategy(tolerance=1e-12, max_bond_dimension=256)
+    out = {"split_case": [m, n], "steps": args.steps}
+    for form in ("plain", "mixed"):
+        sg.set_precision("fp64" if form == "plain" else "mixed")
+        for _ in range(max(1, args.warmup)):
+            core._left_orth_2site(AA, st)
+        torch.cuda.synchronize()
+        _lib.stats_reset()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            U, SV, err = core._left_orth_2site(AA, st)
+        e1.record()
+        e1.synchronize()
+        stt = _lib.stats_read()
+        out[form] = {"ms_per_split": e0.elapsed_time(e1) / args.steps, "D": int(U.shape[-1]),
+                     "err": float(err), "launches_per_split": stt["launches"] / args.steps,
+                     "mixed_fallbacks": stt["mixed_fallbacks"],
+                     "jacobi_sweeps_per_split": stt["jacobi_sweeps"] / args.steps}
+    sg.set_precision("fp64")
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -211,9 +257,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=30)
     ap.add_argument("--chi", type=int, default=256)
-    ap.add_argument("--form", default="plain", choices=["plain"])
+    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--split-case", type=int, nargs=2, metavar=("M", "N"),
+                    help="time single M x N two-site splits in both precision modes and exit")
     args = ap.parse_args()
+    if args.split_case:
+        return run_split_case(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -237,6 +287,7 @@ def main():
 
     mps_h, mpo_h = make_workload(args.n, args.chi)
     st = sg.DEFAULT_STRATEGY.replace(**strategy_kwargs(args.chi))
+    sg.set_precision("fp64" if args.form == "plain" else "mixed")
     psi = sg.MPS(mps_h)
     O = sg.MPO(mpo_h, st)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -266,7 +317,8 @@ def main():
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
-    launches = _lib.stats_read()["launches"]
+    timed_stats = _lib.stats_read()
+    launches = timed_stats["launches"]
     total_ms = sum(times)
     if dist:
         t = torch.tensor([total_ms], device="cuda")
@@ -324,11 +376,19 @@ def main():
 
     # ---- CPU baseline (oracle, bounded sample) -------------------------------
     cpu = None
+    oracle_check = None
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import seemps_oracle as so
 
         try:
-            t, s = cpu_run(mps_h, mpo_h, args.chi)
+            t, s, res = cpu_run(mps_h, mpo_h, args.chi, want_result=True)
+            import numpy as _np
+
+            out_np = [x.detach().cpu().numpy() for x in out._data]
+            oracle_check = {"fidelity_error_vs_oracle": float(so.fidelity_error(out_np, res.tensors)),
+                            "error_bound": float(out.error()), "oracle_error_bound": float(res.error),
+                            "bonds_equal": out.bond_dimensions()[:-1] == [x.shape[0] for x in res.tensors]}
+            del _np
             cpu = {"value": s / t, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": "one full MPO.apply+simplify call of this workload (2 sweeps), "
                              f"{t:.1f} s; NumPy/SciPy BLAS+LAPACK restatement of the reference "
@@ -341,14 +401,23 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.form == "plain" else "f32+f64",
             "data": "synthetic", "config": workload_config(args),
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches, "bonds_out": out.bond_dimensions()[: args.n // 2 + 1],
-            "error": out.error(),
+            "error": out.error(), "oracle_check": oracle_check,
         }
+        if args.form == "mixed":
+            k = max(1, args.steps)
+            line["mixed"] = {
+                "splits_per_step": timed_stats["mixed_splits"] / k,
+                "fallbacks_per_step": timed_stats["mixed_fallbacks"] / k,
+                "rows_per_split": timed_stats["mixed_rows"] / max(1, timed_stats["mixed_splits"]),
+                "cluster_ms_per_step": stt["cluster_ms"],
+            }
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -87,6 +87,34 @@ const char* sm_last_error(void);
 int sm_ctx_create(void** ctx, int device);
 int sm_ctx_destroy(void* ctx);
 
+/* Arithmetic of the splits run through this context (no reference
+ * counterpart: the reference always computes in FP64).
+ *   SM_PRECISION_FP64  (default) every split is the FP64 Jacobi SVD; ranks and
+ *                      singular values follow the reference's gesdd.
+ *   SM_PRECISION_MIXED the one-isometry splits of canonical updates and
+ *                      simplify sweeps (k >= 24) run an FP32 rank-revealing QR
+ *                      + Jacobi inside one 16-CTA cluster, refined by FP64 GEMMs
+ *                      against the exact matrix; the discarded weight is exact
+ *                      in FP64 and the split falls back to SM_PRECISION_FP64
+ *                      when it exceeds the strategy's tolerance with fewer
+ *                      than max_bond_dimension values kept.  Ranks may differ
+ *                      from the reference's at the tolerance boundary. */
+enum { SM_PRECISION_FP64 = 0, SM_PRECISION_MIXED = 1 };
+int sm_ctx_set_precision(void* ctx, int precision);
+
+/* Kernel-level entry of the mixed split's FP32 stage (no reference
+ * counterpart; for unit tests of that stage): rank-revealing QR + one-sided
+ * Jacobi of W = (want_u ? A^T : A), A m x n on the device, inside one 16-CTA
+ * cluster.  Writes kcap >= min(m,n) + 32 rows of length l (= m if want_u else
+ * n) to `rows` (FP64 / complex128, in no particular order, mutually orthogonal
+ * to FP32 accuracy, spanning W's row space; zero past *keff) and their norms
+ * (= singular values of W) to `nrm`.  *keff = rows the QR kept; *sweeps =
+ * Jacobi sweeps.  SM_ERR_VALUE when the sizes exceed the cluster's capacity,
+ * SM_ERR_LINALG when the iteration did not converge. */
+int sm_split_rows_f32(void* ctx, int dtype, const void* A, int m, int n, int want_u,
+                      double thr_rel, double thr_abs, void* rows, double* nrm, int kcap,
+                      int* keff, int* sweeps, void* stream);
+
 /* ---- kernel table (replaces seemps.cython, cython/__init__.py:25-54) ----- */
 
 /* destructively_truncate_vector (cython/truncation.pxi:329-334): s_dev holds n
@@ -204,6 +232,10 @@ typedef struct sm_stats {
   double jacobi_flops;     /* algorithmic SVD flops of those launches */
   double gemm_ms;          /* event-timed device time of the GEMMs */
   double gemm_flops;
+  int64_t mixed_splits;    /* splits attempted in SM_PRECISION_MIXED */
+  int64_t mixed_fallbacks; /* of those, redone by the FP64 path */
+  int64_t mixed_rows;      /* rows of R carried into the cluster Jacobi, summed */
+  double cluster_ms;       /* event-timed device time of the cluster kernel */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

@@ -60,6 +60,10 @@ class sm_stats(C.Structure):
         ("jacobi_flops", C.c_double),
         ("gemm_ms", C.c_double),
         ("gemm_flops", C.c_double),
+        ("mixed_splits", C.c_int64),
+        ("mixed_fallbacks", C.c_int64),
+        ("mixed_rows", C.c_int64),
+        ("cluster_ms", C.c_double),
     ]
 
 
@@ -75,6 +79,9 @@ SIGNATURES = {
     "sm_last_error": (C.c_char_p, []),
     "sm_ctx_create": (C.c_int, [C.POINTER(vp), C.c_int]),
     "sm_ctx_destroy": (C.c_int, [vp]),
+    "sm_ctx_set_precision": (C.c_int, [vp, C.c_int]),
+    "sm_split_rows_f32": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_double,
+                                    C.c_double, vp, dp, C.c_int, ip, ip, vp]),
     "sm_truncate": (C.c_int, [vp, vp, C.c_int, stp, ip, dp, vp]),
     "sm_gemm": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int,
                           vp, C.c_int, vp, C.c_int, vp]),
@@ -225,6 +232,17 @@ class SplitTrace:
         offs = np.concatenate([[0], np.cumsum([lens[k] for k in range(n.value)])]).astype(int)
         self.s = [allv[offs[k]:offs[k + 1]] for k in range(n.value)]
         return False
+
+
+PRECISIONS = {"fp64": 0, "mixed": 1}
+
+
+def set_precision(mode: str, device: int = 0) -> None:
+    """Arithmetic of the SVD splits: "fp64" (default, reference ranks) or
+    "mixed" (FP32 cluster factorisation refined by FP64 GEMMs)."""
+    if mode not in PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {mode!r}")
+    check(load().sm_ctx_set_precision(context(device), PRECISIONS[mode]))
 
 
 def stats_reset(timing: bool = False, device: int = 0):

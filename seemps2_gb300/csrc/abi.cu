@@ -182,6 +182,57 @@ int sm_ctx_destroy(void* ctx) {
   return SM_OK;
 }
 
+int sm_ctx_set_precision(void* ctx, int precision) {
+  SM_GUARD_CTX(ctx);
+  if (precision != SM_PRECISION_FP64 && precision != SM_PRECISION_MIXED) {
+    set_error("sm_ctx_set_precision: unknown precision mode");
+    return SM_ERR_VALUE;
+  }
+  as_ctx(ctx)->precision = precision;
+  return SM_OK;
+}
+
+int sm_split_rows_f32(void* ctx, int dtype, const void* A, int m, int n, int want_u,
+                      double thr_rel, double thr_abs, void* rows, double* nrm, int kcap,
+                      int* keff, int* sweeps, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (!A || !rows || !nrm || !keff || !sweeps || m < 1 || n < 1 || kcap < std::min(m, n) + 32) {
+    set_error("sm_split_rows_f32: need m, n >= 1, kcap >= min(m, n) + 32 and non-null pointers");
+    return SM_ERR_VALUE;
+  }
+  Ctx& c = *as_ctx(ctx);
+  cudaStream_t st = as_stream(stream);
+  const int kw = want_u ? n : m, l = want_u ? m : n;
+  const bool fits = dtype == SM_FLOAT64 ? split_cluster_fits<double>(kw, l)
+                                        : split_cluster_fits<cplx>(kw, l);
+  if (!fits) {
+    set_error("sm_split_rows_f32: matrix exceeds the cluster's capacity");
+    return SM_ERR_VALUE;
+  }
+  JacobiCtl* ctl;
+  double* info;
+  SM_CHECK(c.scratch("rows.ctl", 1, &ctl));
+  SM_CHECK(c.scratch("rows.info", 4, &info));
+  SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
+  if (dtype == SM_FLOAT64)
+    SM_CHECK(split_cluster_f32<double>(st, (const double*)A, m, n, want_u != 0, thr_rel, thr_abs,
+                                       60, (double*)rows, nrm, kcap, ctl, info));
+  else
+    SM_CHECK(split_cluster_f32<cplx>(st, (const cplx*)A, m, n, want_u != 0, thr_rel, thr_abs, 60,
+                                     (cplx*)rows, nrm, kcap, ctl, info));
+  JacobiCtl* h = reinterpret_cast<JacobiCtl*>(c.pinned);
+  SM_CUDA_CHECK(cudaMemcpyAsync(h, ctl, sizeof(JacobiCtl), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  *keff = h->nact;
+  *sweeps = h->sweeps;
+  if (h->status != 0) {
+    set_error("sm_split_rows_f32: the FP32 Jacobi iteration did not converge");
+    return SM_ERR_LINALG;
+  }
+  return SM_OK;
+}
+
 int sm_truncate(void* ctx, const double* s_dev, int n, const sm_strategy* st, int* rank,
                 double* err2, void* stream) {
   SM_GUARD_CTX(ctx);
@@ -201,11 +252,12 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const v
     set_error("sm_gemm: invalid op flag");
     return SM_ERR_VALUE;
   }
+  // through the context: split-K for small outputs, counted in the stats
   if (dtype == SM_FLOAT64)
-    return gemm<double>(as_stream(stream), opA, opB, M, N, K, 1.0, (const double*)A, lda,
-                        (const double*)B, ldb, 0.0, (double*)C, ldc);
-  return gemm<cplx>(as_stream(stream), opA, opB, M, N, K, cplx{1.0, 0.0}, (const cplx*)A, lda,
-                    (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc);
+    return gemm_ctx<double>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K, 1.0,
+                            (const double*)A, lda, (const double*)B, ldb, 0.0, (double*)C, ldc);
+  return gemm_ctx<cplx>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K, cplx{1.0, 0.0},
+                        (const cplx*)A, lda, (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc);
 }
 
 int sm_svd(void* ctx, int dtype, const void* A, int m, int n, void* U, double* s, void* Vt,

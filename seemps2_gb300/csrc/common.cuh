@@ -41,6 +41,8 @@ template <> struct S<double> {
   // c + conj(a) * b
   __host__ __device__ static double cfma(double a, double b, double c) { return ::fma(a, b, c); }
   __host__ __device__ static double scale(double a, double s) { return a * s; }
+  __host__ __device__ static double from_real(double a) { return a; }
+  __host__ __device__ static double neg(double a) { return -a; }
 };
 template <> struct S<cplx> {
   static constexpr int kDtype = SM_COMPLEX128;
@@ -56,6 +58,8 @@ template <> struct S<cplx> {
     return {::fma(a.re, b.re, ::fma(a.im, b.im, c.re)), ::fma(a.re, b.im, ::fma(-a.im, b.re, c.im))};
   }
   __host__ __device__ static cplx scale(cplx a, double s) { return {a.re * s, a.im * s}; }
+  __host__ __device__ static cplx from_real(double a) { return {a, 0.0}; }
+  __host__ __device__ static cplx neg(cplx a) { return {-a.re, -a.im}; }
 };
 
 // ---------------------------------------------------------------------------

@@ -7,7 +7,13 @@
 // runs FP64 on the CUDA cores only, so this is a shared-memory tiled SIMT
 // kernel: 64x64 output tile per CTA, 16-deep K slices, 256 threads holding a
 // 4x4 register tile each; the FP64 pipe is the bound, not HBM (operands are
-// re-read from L2 at most M/64 + N/64 times).
+// re-read from L2 at most M/64 + N/64 times).  When the output has fewer
+// tiles than the GPU has SMs (the 256..768-sized contractions of a sweep give
+// 16-150 tiles), the K range is split over blockIdx.z: each slice writes its
+// partial tile to a workspace and a second kernel sums the slices in a fixed
+// order (deterministic) and applies alpha / beta.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace sm {
@@ -31,7 +37,8 @@ template <typename T>
 __global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int K, T alpha,
                                              const T* __restrict__ A, int lda,
                                              const T* __restrict__ B, int ldb, T beta,
-                                             T* __restrict__ C, int ldc) {
+                                             T* __restrict__ C, int ldc, int kchunk,
+                                             T* __restrict__ part) {
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
   const int tid = threadIdx.x;
@@ -43,7 +50,9 @@ __global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = S<T>::zero();
 
-  for (int k0 = 0; k0 < K; k0 += BK) {
+  const int kbeg = blockIdx.z * kchunk;
+  const int kend = min(K, kbeg + kchunk);
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
 #pragma unroll
     for (int e = 0; e < (BM * BK) / NT; ++e) {
       const int idx = tid + e * NT;
@@ -52,7 +61,7 @@ __global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int
       else                { kk = idx / BM; mm = idx % BM; }
       const int gm = m0 + mm, gk = k0 + kk;
       T v = S<T>::zero();
-      if (gm < M && gk < K)
+      if (gm < M && gk < kend)
         v = opA == SM_OP_N ? load_op(A + (size_t)gm * lda + gk, opA)
                            : load_op(A + (size_t)gk * lda + gm, opA);
       As[kk][mm] = v;
@@ -65,7 +74,7 @@ __global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int
       else                { nn = idx / BK; kk = idx % BK; }
       const int gn = n0 + nn, gk = k0 + kk;
       T v = S<T>::zero();
-      if (gn < N && gk < K)
+      if (gn < N && gk < kend)
         v = opB == SM_OP_N ? load_op(B + (size_t)gk * ldb + gn, opB)
                            : load_op(B + (size_t)gn * ldb + gk, opB);
       Bs[kk][nn] = v;
@@ -85,6 +94,20 @@ __global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int
     }
     __syncthreads();
   }
+  if (part) {
+    T* p = part + (size_t)blockIdx.z * M * N;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int gm = m0 + ty + 16 * i;
+      if (gm >= M) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int gn = n0 + tx + 16 * j;
+        if (gn < N) p[(size_t)gm * N + gn] = acc[i][j];
+      }
+    }
+    return;
+  }
   const bool use_beta = S<T>::abs2(beta) != 0.0;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -99,6 +122,24 @@ __global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int
       if (use_beta) v = S<T>::fma(beta, *c, v);
       *c = v;
     }
+  }
+}
+
+// C = alpha * sum_z part[z] + beta * C, slices summed in order z = 0, 1, ...
+template <typename T>
+__global__ void k_splitk_reduce(int M, int N, int nz, const T* __restrict__ part, T alpha, T beta,
+                                T* __restrict__ C, int ldc) {
+  const bool use_beta = S<T>::abs2(beta) != 0.0;
+  const size_t mn = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < mn;
+       e += (size_t)gridDim.x * blockDim.x) {
+    T acc = part[e];
+    for (int z = 1; z < nz; ++z) acc = acc + part[(size_t)z * mn + e];
+    const int gm = (int)(e / N), gn = (int)(e % N);
+    T* c = C + (size_t)gm * ldc + gn;
+    T v = alpha * acc;
+    if (use_beta) v = S<T>::fma(beta, *c, v);
+    *c = v;
   }
 }
 
@@ -121,10 +162,40 @@ int gemm(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const 
     set_error("gemm: M too large");
     return SM_ERR_VALUE;
   }
-  k_gemm<T><<<grid, NT, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  k_gemm<T><<<grid, NT, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, K,
+                                 nullptr);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
+}
+
+// Split-K variant: `nz` K slices (nz > 1) through the workspace `part`
+// (nz * M * N elements).
+template <typename T>
+int gemm_splitk(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A,
+                int lda, const T* B, int ldb, T beta, T* C, int ldc, int nz, T* part) {
+  const int kchunk = ((K + nz - 1) / nz + BK - 1) / BK * BK;
+  nz = (K + kchunk - 1) / kchunk;
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, nz);
+  k_gemm<T><<<grid, NT, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk,
+                                 part);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  const size_t mn = (size_t)M * N;
+  const int blocks = (int)std::min<size_t>((mn + 255) / 256, 4096);
+  k_splitk_reduce<T><<<blocks, 256, 0, st>>>(M, N, nz, part, alpha, beta, C, ldc);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
+}
+
+// K slices for an M x N x K product on `sms` SMs: enough CTAs for about two
+// waves, each slice at least 64 deep; 1 = no split.
+int splitk_slices(int M, int N, int K, int sms) {
+  const long tiles = (long)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+  if (tiles >= sms || K < 128) return 1;
+  const long want = (2L * sms + tiles - 1) / tiles;
+  return (int)std::max(1L, std::min({want, (long)(K / 64), 32L}));
 }
 
 template <typename T>
@@ -133,9 +204,17 @@ int gemm_ctx(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T
   if (M == 0 || N == 0 || K == 0) return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   ctx.stats.gemm_launches += 1;
   ctx.stats.gemm_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
-  if (!ctx.timing) return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  const int nz = splitk_slices(M, N, K, std::max(1, ctx.num_sms));
+  T* part = nullptr;
+  if (nz > 1) SM_CHECK(ctx.scratch("gemm.splitk", (size_t)nz * M * N, &part));
+  auto run = [&]() -> int {
+    if (nz > 1)
+      return gemm_splitk<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nz, part);
+    return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  };
+  if (!ctx.timing) return run();
   SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
-  SM_CHECK(gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc));
+  SM_CHECK(run());
   SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
   SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
   float ms = 0.f;

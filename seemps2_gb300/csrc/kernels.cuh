@@ -16,6 +16,7 @@ namespace sm {
 struct Ctx {
   int device = 0;
   int num_sms = 0;
+  int precision = 0;  // SM_PRECISION_FP64 or SM_PRECISION_MIXED
   void* pinned = nullptr;  // 64 KB of pinned host memory
   std::map<std::string, std::pair<void*, size_t>> bufs;
   std::map<const void*, int> coop_blocks;  // per-kernel co-resident CTA limit
@@ -46,6 +47,18 @@ struct SplitResult {
   int status;
   double err2;
   int sweeps;
+  int pad;
+};
+
+// Control block of one Jacobi iteration: grid-barrier words, convergence
+// status (DevStatus bits) and the sweep count.
+struct JacobiCtl {
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  unsigned int rot[2];
+  int status;
+  int sweeps;
+  int nact;  // rows still taking part in the iteration (deflation / rank)
   int pad;
 };
 
@@ -100,5 +113,18 @@ template <typename T>
 int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
               int left_mode, T* left, int right_mode, T* right, double* s_out,
               SplitResult* res);
+
+// --- svd_mixed.cu ------------------------------------------------------------
+// Whether the 16-CTA cluster factorisation holds W (kw x l) on this GPU.
+template <typename T>
+bool split_cluster_fits(int kw, int l);
+// FP32 rank-revealing QR + one-sided Jacobi of W = (want_u ? A^T : A) in one
+// cluster.  Writes kcap rows (FP64, ld = l, zero past the iteration's rows)
+// and their norms; ctl receives status / sweeps / nact = rows of R kept;
+// info[0] = |A|_F^2 (FP64), info[1] = trailing weight dropped by the QR.
+template <typename T>
+int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
+                      double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
+                      JacobiCtl* ctl, double* info);
 
 }  // namespace sm

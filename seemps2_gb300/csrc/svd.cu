@@ -32,16 +32,6 @@ namespace sm {
 
 namespace {
 
-struct JacobiCtl {
-  unsigned int bar_count;
-  unsigned int bar_gen;
-  unsigned int rot[2];
-  int status;
-  int sweeps;
-  int nact;  // rows still taking part in the iteration (deflation)
-  int pad;
-};
-
 // Grid-wide barrier with a bounded spin: one arrival counter and a generation
 // word (measured on GB300: ~2.3 us for 16-256 CTAs, cheaper than per-CTA
 // arrival flags gathered by one CTA).  Returns false (and sets the status
@@ -1048,6 +1038,381 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   return SM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-precision split (SM_PRECISION_MIXED): the cluster kernel of
+// svd_mixed.cu gives the right singular vectors of W to FP32 accuracy; FP64
+// GEMMs then refine them with the exact matrix:
+//   1. the rows, normalised, are approximate eigenvectors of W^H W within the
+//      row space the FP32 QR kept (it drops at most 1% of the weight the
+//      tolerance allows).  A power step (rows of V W^H W) is NOT used: rows
+//      whose sigma is below FP64 resolution relative to sigma_max would turn
+//      into rounding-level copies of the dominant directions.
+//   2. refinement of the approximate eigenvectors of W^H W (Ogita & Aishima,
+//      "Iterative refinement for symmetric eigenvalue decomposition", Japan J.
+//      Indust. Appl. Math. 35 (2018)): with G = V W^H W V^H and M = V V^H,
+//      lambda_i = G_ii / M_ii, R = I - M,
+//        E_ij = (G_ij + lambda_j R_ij) / (lambda_j - lambda_i)   (|E_ij| <= 1/4)
+//        E_ij = R_ij / 2                                         (otherwise)
+//      and V <- (I + E)^H V.  Each step squares the error for separated pairs;
+//      nearly degenerate pairs are only re-orthonormalised, which leaves the
+//      subspace they span unchanged.
+//   3. sigma_i = |W v_i^H| from the final C = W V^H; the reference truncation
+//      rule on these FP64 values gives D; the discarded weight is computed
+//      exactly as |A|_F^2 - sum_{kept} sigma_i^2.  The factors are V's rows and
+//      C's columns, so the output never has to be formed from A again.
+// The caller falls back to the FP64 split (svd_split_xfree) when the cluster
+// iteration did not converge, when a kept singular value lies below the FP32
+// resolution (1e-4 s_max), when a kept and a dropped direction are still
+// coupled by more than 1e-7 after the refinement (a cut gap below the FP32
+// backward error), or when the exact discarded weight breaks the strategy's
+// tolerance while fewer than max_bond_dimension values are kept.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kMixedMinRank = 24;  // smaller splits stay on the FP64 path
+constexpr int kMixedRefine = 3;    // refinement steps
+constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
+constexpr double kMixedCutAngle = 1e-7;  // largest kept/dropped coupling accepted
+
+template <typename T>
+__global__ void k_gather_rows(const T* __restrict__ rows, int l, const int* __restrict__ perm,
+                              const double* __restrict__ s, int cnt, T* __restrict__ dst) {
+  const size_t tot = (size_t)cnt * l;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / l), x = (int)(e % l);
+    const double si = s[i];
+    dst[e] = si > 0.0 ? S<T>::scale(rows[(size_t)perm[i] * l + x], 1.0 / si) : S<T>::zero();
+  }
+}
+
+// X[i] /= nrm[i] (zero rows stay zero)
+template <typename T>
+__global__ void k_scale_rows(T* __restrict__ X, int k, int l, const double* __restrict__ nrm) {
+  const size_t tot = (size_t)k * l;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double r = nrm[e / l];
+    X[e] = r > 0.0 ? S<T>::scale(X[e], 1.0 / r) : S<T>::zero();
+  }
+}
+
+__device__ __forceinline__ double re_of(double x) { return x; }
+__device__ __forceinline__ double re_of(cplx x) { return x.re; }
+
+// F = (I + E)^H from G and M (k x k, Hermitian), E as described above.
+// Pairs of rows that are both below FP32 resolution (lambda < blind2 *
+// lambda_0; row 0 has the largest norm) are left alone (E = 0): their FP32
+// directions are rounding noise, a first-order correction between them is
+// meaningless and would break their orthogonality; they are still decoupled
+// from the resolved rows.
+template <typename T>
+__global__ void k_refine_matrix(const T* __restrict__ G, const T* __restrict__ M, int k,
+                                double blind2, T* __restrict__ F) {
+  const double m00 = re_of(M[0]);
+  const double lmax = m00 > 0.0 ? re_of(G[0]) / m00 : 0.0;
+  const size_t tot = (size_t)k * k;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / k), j = (int)(e % k);
+    // F_ij = delta_ij + conj(E_ji)
+    const double mii = re_of(M[(size_t)i * k + i]), mjj = re_of(M[(size_t)j * k + j]);
+    const double li = mii > 0.0 ? re_of(G[(size_t)i * k + i]) / mii : 0.0;
+    const double lj = mjj > 0.0 ? re_of(G[(size_t)j * k + j]) / mjj : 0.0;
+    T Eji;
+    if (i == j) {
+      Eji = S<T>::from_real(0.5 * (1.0 - mii));
+    } else if (li < blind2 * lmax && lj < blind2 * lmax) {
+      Eji = S<T>::zero();
+    } else {
+      const T r = S<T>::neg(M[(size_t)j * k + i]);  // R_ji = -M_ji
+      const T num = G[(size_t)j * k + i] + S<T>::scale(r, li);
+      const double gap = li - lj;
+      if (gap != 0.0 && 16.0 * S<T>::abs2(num) <= gap * gap) Eji = S<T>::scale(num, 1.0 / gap);
+      else Eji = S<T>::scale(r, 0.5);
+    }
+    T f = S<T>::conj(Eji);
+    if (i == j) f = f + S<T>::one();
+    F[e] = f;
+  }
+}
+
+// F = 1.5 I - 0.5 M: one Newton-Schulz step X <- F X towards orthonormal rows.
+template <typename T>
+__global__ void k_ns_matrix(const T* __restrict__ M, int k, T* __restrict__ F) {
+  const size_t tot = (size_t)k * k;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    T f = S<T>::scale(M[e], -0.5);
+    if (e / k == e % k) f = f + S<T>::from_real(1.5);
+    F[e] = f;
+  }
+}
+
+// out[j] = |C[:, j]| for C (rows x cols, row-major)
+template <typename T>
+__global__ void k_col_norms(const T* __restrict__ C, int rows, int cols, double* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cols) return;
+  double a = 0.0;
+  for (int i = 0; i < rows; ++i) a += S<T>::abs2(C[(size_t)i * cols + j]);
+  out[j] = sqrt(a);
+}
+
+// Exact discarded weight |A|^2 - sum_{j<D} s_j^2 into the split result.
+// Also info[2] = s[0], info[3] = s[D-1] for the host's checks.
+__global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, double* info) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double kept = 0.0;
+  for (int j = 0; j < res->D; ++j) kept += s[j] * s[j];
+  res->err2 = fmax(0.0, info[0] - kept);
+  info[2] = s[0];
+  info[3] = s[max(res->D, 1) - 1];
+}
+
+// Largest coupling angle |G_ij| / (lambda_i - lambda_j) left between a kept
+// row i and a dropped row j after the refinement (G = C^H C of the final rows,
+// lambda = s^2 in sorted order): the a-posteriori check that the kept
+// subspace is resolved to FP64 accuracy.  Writes info[4].
+template <typename T>
+__global__ void k_cut_check(const T* __restrict__ G, int cnt, const int* __restrict__ perm,
+                            const double* __restrict__ s, const SplitResult* res, double* info) {
+  __shared__ double red[256];
+  const int D = res->D;
+  double worst = 0.0;
+  const long pairs = (long)D * (cnt - D);
+  for (long e = threadIdx.x; e < pairs; e += blockDim.x) {
+    const int a = (int)(e / (cnt - D)), b = D + (int)(e % (cnt - D));
+    const double gap = s[a] * s[a] - s[b] * s[b];
+    const double g = sqrt(S<T>::abs2(G[(size_t)perm[a] * cnt + perm[b]]));
+    const double th = gap > 0.0 ? g / gap : (g > 0.0 ? 1e300 : 0.0);
+    worst = fmax(worst, th);
+  }
+  red[threadIdx.x] = worst;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) info[4] = red[0];
+}
+
+// Factors from the refined rows V (cnt x l) and C = W V^H (kw x cnt).
+template <typename T>
+__global__ void k_emit_mixed(int want_u, int m, int n, int D, const T* __restrict__ V, int l,
+                             const T* __restrict__ C, int cnt, const int* __restrict__ perm,
+                             T* __restrict__ iso, T* __restrict__ oth) {
+  const size_t niso = want_u ? (size_t)m * D : (size_t)D * n;
+  const size_t noth = want_u ? (size_t)D * n : (size_t)m * D;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < niso + noth;
+       e += (size_t)gridDim.x * blockDim.x) {
+    if (e < niso) {
+      if (want_u) {  // U[i][j] = V[perm j][i]
+        const int i = (int)(e / D), j = (int)(e % D);
+        iso[e] = V[(size_t)perm[j] * l + i];
+      } else {  // Vh[j][x] = V[perm j][x]
+        const int j = (int)(e / n), x = (int)(e % n);
+        iso[e] = V[(size_t)perm[j] * l + x];
+      }
+    } else {
+      const size_t f = e - niso;
+      if (want_u) {  // SV[j][x] = C[x][perm j]
+        const int j = (int)(f / n), x = (int)(f % n);
+        oth[f] = C[(size_t)x * cnt + perm[j]];
+      } else {  // US[i][j] = C[i][perm j]
+        const int i = (int)(f / D), j = (int)(f % D);
+        oth[f] = C[(size_t)i * cnt + perm[j]];
+      }
+    }
+  }
+}
+
+inline int grid_for(size_t tot) { return (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, 4096)); }
+
+// Largest discarded weight the strategy allows with D of k values kept
+// (the exact check that sends a mixed split back to the FP64 path).
+double allowed_discard(const sm_strategy& st, double norm2, double s0, int k, int D) {
+  const int drop = std::max(0, k - D);
+  switch (st.method) {
+    case SM_RELATIVE_NORM_SQUARED_ERROR: return st.tolerance * norm2;
+    case SM_RELATIVE_SINGULAR_VALUE: return drop * (st.tolerance * s0) * (st.tolerance * s0);
+    case SM_ABSOLUTE_SINGULAR_VALUE: return drop * st.tolerance * st.tolerance;
+    default: return 0.0;
+  }
+}
+
+}  // namespace
+
+template <typename T>
+int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
+                    bool want_u, T* left, T* right, SplitResult* out, bool* done) {
+  *done = false;
+  const int kw = want_u ? n : m;
+  const int l = want_u ? m : n;
+  const int k = std::min(kw, l);
+  if (k < kMixedMinRank || strat.method == SM_DO_NOT_TRUNCATE || strat.tolerance <= 0.0)
+    return SM_OK;
+  if (!split_cluster_fits<T>(kw, l)) return SM_OK;
+  const int kcap = k + 32;  // the Jacobi writes 32 blocks of ceil(rows / 32)
+  T *rows, *V0, *V1, *Cb, *Gb, *Mb, *Fb;
+  double *nrm, *s_sorted, *errors, *info, *cn;
+  int* perm;
+  JacobiCtl* ctl;
+  SplitResult* res;
+  SM_CHECK(ctx.scratch("mx.rows", (size_t)kcap * l, &rows));
+  SM_CHECK(ctx.scratch("mx.nrm", (size_t)kcap, &nrm));
+  SM_CHECK(ctx.scratch("mx.s", (size_t)kcap, &s_sorted));
+  SM_CHECK(ctx.scratch("mx.err", (size_t)kcap + 1, &errors));
+  SM_CHECK(ctx.scratch("mx.perm", (size_t)kcap, &perm));
+  SM_CHECK(ctx.scratch("mx.info", 8, &info));
+  SM_CHECK(ctx.scratch("mx.ctl", 1, &ctl));
+  SM_CHECK(ctx.scratch("mx.res", 1, &res));
+  // RRQR stop: drop at most 1% of what the tolerance allows (never more than
+  // 1e-10 of |A|^2, which the power step then suppresses further)
+  double thr_rel = 0.0, thr_abs = 0.0;
+  if (strat.method == SM_RELATIVE_NORM_SQUARED_ERROR) thr_rel = std::min(1e-10, 1e-2 * strat.tolerance);
+  else if (strat.method == SM_RELATIVE_SINGULAR_VALUE)
+    thr_rel = std::min(1e-10, 1e-2 * strat.tolerance * strat.tolerance);
+  else thr_abs = 1e-2 * strat.tolerance * strat.tolerance;
+  SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
+  if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+  SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
+                                info));
+  if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+  struct Head {
+    JacobiCtl c;
+    double info[2];
+  };
+  Head* h = reinterpret_cast<Head*>(ctx.pinned);
+  SM_CUDA_CHECK(cudaMemcpyAsync(&h->c, ctl, sizeof(JacobiCtl), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaMemcpyAsync(h->info, info, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  const double norm2 = h->info[0];  // the pinned block is reused below
+  const JacobiCtl hc = h->c;
+  ctx.stats.mixed_splits += 1;
+  if (ctx.timing) {
+    float ms = 0.f;
+    SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+    ctx.stats.cluster_ms += ms;
+  }
+  ctx.stats.jacobi_sweeps += hc.sweeps;
+  if (hc.status != 0) {
+    ctx.stats.mixed_fallbacks += 1;
+    return SM_OK;
+  }
+  const int cnt = std::max(1, std::min(hc.nact, k));
+  ctx.stats.mixed_rows += cnt;
+  SM_CHECK(ctx.scratch("mx.V0", (size_t)cnt * l, &V0));
+  SM_CHECK(ctx.scratch("mx.V1", (size_t)cnt * l, &V1));
+  SM_CHECK(ctx.scratch("mx.C", (size_t)kw * cnt, &Cb));
+  SM_CHECK(ctx.scratch("mx.G", (size_t)cnt * cnt, &Gb));
+  SM_CHECK(ctx.scratch("mx.M", (size_t)cnt * cnt, &Mb));
+  SM_CHECK(ctx.scratch("mx.F", (size_t)cnt * cnt, &Fb));
+  SM_CHECK(ctx.scratch("mx.cn", (size_t)cnt, &cn));
+  // rows by decreasing norm, normalised
+  const size_t sort_smem = sizeof(unsigned long long) * (size_t)kcap;
+  if (sort_smem > 48 * 1024)
+    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sort_smem));
+  k_sort_truncate<<<1, 1024, sort_smem, st>>>(nrm, kcap, strat, perm, s_sorted, errors, ctl, res);
+  note_launch();
+  k_gather_rows<T><<<grid_for((size_t)cnt * l), 256, 0, st>>>(rows, l, perm, s_sorted, cnt, V0);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  const T one = S<T>::one(), zero = S<T>::zero();
+  // C = W V^H (kw x cnt)
+  auto w_vh = [&](const T* V, T* C) -> int {
+    if (want_u) return gemm_ctx<T>(ctx, st, SM_OP_T, SM_OP_C, n, cnt, m, one, A, n, V, m, zero, C, cnt);
+    return gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, m, cnt, n, one, A, n, V, n, zero, C, cnt);
+  };
+  auto normalise = [&](T* X) -> int {
+    k_row_norms<T><<<(cnt + 7) / 8, 256, 0, st>>>(X, l, cnt, l, cn, 0);
+    note_launch();
+    k_scale_rows<T><<<grid_for((size_t)cnt * l), 256, 0, st>>>(X, cnt, l, cn);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    return SM_OK;
+  };
+  // 2. refinement (V0 holds the normalised FP32 rows)
+  T* V = V0;
+  T* Vn = V1;
+  for (int it = 0; it < kMixedRefine; ++it) {
+    SM_CHECK(w_vh(V, Cb));
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, cnt, cnt, l, one, V, l, V, l, zero, Mb, cnt));
+    k_refine_matrix<T><<<grid_for((size_t)cnt * cnt), 256, 0, st>>>(Gb, Mb, cnt,
+                                                                    kMixedBlind * kMixedBlind, Fb);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_N, cnt, l, cnt, one, Fb, cnt, V, l, zero, Vn, l));
+    std::swap(V, Vn);
+  }
+  // Newton-Schulz: orthonormality error e -> 1.5 e^2
+  SM_CHECK(normalise(V));
+  SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, cnt, cnt, l, one, V, l, V, l, zero, Mb, cnt));
+  k_ns_matrix<T><<<grid_for((size_t)cnt * cnt), 256, 0, st>>>(Mb, cnt, Fb);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_N, cnt, l, cnt, one, Fb, cnt, V, l, zero, Vn, l));
+  std::swap(V, Vn);
+  SM_CHECK(normalise(V));
+  // 3. singular values, truncation, exact discarded weight
+  SM_CHECK(w_vh(V, Cb));
+  k_col_norms<T><<<(cnt + 127) / 128, 128, 0, st>>>(Cb, kw, cnt, cn);
+  note_launch();
+  const size_t smem2 = sizeof(unsigned long long) * (size_t)cnt;
+  k_sort_truncate<<<1, 1024, smem2, st>>>(cn, cnt, strat, perm, s_sorted, errors, ctl, res);
+  note_launch();
+  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info);
+  note_launch();
+  SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
+  k_cut_check<T><<<1, 256, 0, st>>>(Gb, cnt, perm, s_sorted, res, info);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  SplitResult* hr = reinterpret_cast<SplitResult*>(ctx.pinned);
+  SM_CUDA_CHECK(cudaMemcpyAsync(hr, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
+  double* hs = reinterpret_cast<double*>(hr + 1);
+  SM_CUDA_CHECK(cudaMemcpyAsync(hs, info + 2, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  const double s0 = hs[0];
+  const SplitResult r = *hr;
+  const int D = r.D;
+  // FP32 resolves a singular vector only down to ~1e-4 s_max (the refinement
+  // needs the FP32 error below 1/4 of the relative gap): a cut below that, or a
+  // discarded weight beyond the tolerance with fewer than max_bond values
+  // kept, sends the split to the FP64 path.
+  const double s_last = hs[1];
+  const double cut_angle = hs[2];
+  if (s_last < kMixedBlind * s0 || !(cut_angle <= kMixedCutAngle) ||
+      (D < strat.max_bond_dimension && D < k &&
+       r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12))) {
+    ctx.stats.mixed_fallbacks += 1;
+    return SM_OK;
+  }
+  T* iso = want_u ? left : right;
+  T* oth = want_u ? right : left;
+  const size_t tot = (size_t)D * (m + n);
+  k_emit_mixed<T><<<grid_for(tot), 256, 0, st>>>(want_u ? 1 : 0, m, n, D, V, l, Cb, cnt, perm, iso,
+                                                 oth);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  *out = r;
+  out->status = 0;
+  ctx.stats.splits += 1;
+  if (ctx.trace) {
+    const size_t off = ctx.tr_s.size();
+    ctx.tr_s.resize(off + cnt);
+    SM_CUDA_CHECK(cudaMemcpyAsync(ctx.tr_s.data() + off, s_sorted, sizeof(double) * cnt,
+                                  cudaMemcpyDeviceToHost, st));
+    SM_CUDA_CHECK(cudaStreamSynchronize(st));
+    ctx.tr_rank.push_back(D);
+    ctx.tr_len.push_back(cnt);
+    ctx.tr_err2.push_back(r.err2);
+  }
+  *done = true;
+  return SM_OK;
+}
+
 template <typename T>
 int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
               int left_mode, T* left, int right_mode, T* right, double* s_out,
@@ -1056,10 +1421,15 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     set_error("svd: empty matrix");
     return SM_ERR_VALUE;
   }
-  if (left_mode == OUT_U && right_mode == OUT_SVT)
-    return svd_split_xfree<T>(ctx, st, A, m, n, strat, true, left, right, s_out, out);
-  if (left_mode == OUT_US && right_mode == OUT_VT)
-    return svd_split_xfree<T>(ctx, st, A, m, n, strat, false, left, right, s_out, out);
+  const bool xu = left_mode == OUT_U && right_mode == OUT_SVT;
+  const bool xv = left_mode == OUT_US && right_mode == OUT_VT;
+  if ((xu || xv) && ctx.precision == SM_PRECISION_MIXED && !s_out) {
+    bool done = false;
+    SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done));
+    if (done) return SM_OK;
+  }
+  if (xu) return svd_split_xfree<T>(ctx, st, A, m, n, strat, true, left, right, s_out, out);
+  if (xv) return svd_split_xfree<T>(ctx, st, A, m, n, strat, false, left, right, s_out, out);
   const int k = std::min(m, n), l = std::max(m, n);
   const bool wide = m <= n;
   const int ld = l + k;  // rows are [w (l) | x (k)]

@@ -46,7 +46,9 @@ def test_truncation_rule_on_device_is_bit_exact():
 @pytest.mark.parametrize("opB", [0, 1, 2])
 @pytest.mark.parametrize("opA", [0, 1, 2])
 def test_gemm_flags(opA, opB, cplx):
-    for (M, N, K) in [(1, 1, 1), (5, 3, 4), (70, 65, 33), (130, 17, 200)]:
+    # the last three take the split-K path (fewer output tiles than SMs)
+    for (M, N, K) in [(1, 1, 1), (5, 3, 4), (70, 65, 33), (130, 17, 200), (256, 256, 512),
+                      (300, 258, 384), (64, 700, 1000)]:
         A = rand((M, K) if opA == 0 else (K, M), cplx)
         B = rand((K, N) if opB == 0 else (N, K), cplx)
         opn = {0: lambda x: x, 1: lambda x: x.T, 2: lambda x: x.conj().T}
