@@ -244,6 +244,8 @@ def run_split_case(args):
         out[form] = {"ms_per_split": e0.elapsed_time(e1) / args.steps, "D": int(U.shape[-1]),
                      "err": float(err), "launches_per_split": stt["launches"] / args.steps,
                      "mixed_fallbacks": stt["mixed_fallbacks"],
+                     "cluster_qr_ms": stt["cluster_qr_ms"] / args.steps,
+                     "cluster_jacobi_ms": stt["cluster_jacobi_ms"] / args.steps,
                      "jacobi_sweeps_per_split": stt["jacobi_sweeps"] / args.steps}
     sg.set_precision("fp64")
     print(json.dumps(out), flush=True)
@@ -417,6 +419,8 @@ def main():
                 "fallbacks_per_step": timed_stats["mixed_fallbacks"] / k,
                 "rows_per_split": timed_stats["mixed_rows"] / max(1, timed_stats["mixed_splits"]),
                 "cluster_ms_per_step": stt["cluster_ms"],
+                "cluster_qr_ms_per_step": timed_stats["cluster_qr_ms"] / k,
+                "cluster_jacobi_ms_per_step": timed_stats["cluster_jacobi_ms"] / k,
             }
         print(json.dumps(line), flush=True)
     if dist:

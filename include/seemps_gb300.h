@@ -236,6 +236,8 @@ typedef struct sm_stats {
   int64_t mixed_fallbacks; /* of those, redone by the FP64 path */
   int64_t mixed_rows;      /* rows of R carried into the cluster Jacobi, summed */
   double cluster_ms;       /* event-timed device time of the cluster kernel */
+  double cluster_qr_ms;    /* of which: load + FP32 QR (device timer) */
+  double cluster_jacobi_ms;/* of which: FP32 Jacobi + store (device timer) */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

@@ -64,6 +64,8 @@ class sm_stats(C.Structure):
         ("mixed_fallbacks", C.c_int64),
         ("mixed_rows", C.c_int64),
         ("cluster_ms", C.c_double),
+        ("cluster_qr_ms", C.c_double),
+        ("cluster_jacobi_ms", C.c_double),
     ]
 
 

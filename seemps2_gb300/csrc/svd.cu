@@ -1056,23 +1056,27 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
 //      and V <- (I + E)^H V.  Each step squares the error for separated pairs;
 //      nearly degenerate pairs are only re-orthonormalised, which leaves the
 //      subspace they span unchanged.
-//   3. sigma_i = |W v_i^H| from the final C = W V^H; the reference truncation
-//      rule on these FP64 values gives D; the discarded weight is computed
-//      exactly as |A|_F^2 - sum_{kept} sigma_i^2.  The factors are V's rows and
-//      C's columns, so the output never has to be formed from A again.
+//   3. sigma_i = |W v_i^H| from the final C = W V^H.  For the relative-norm
+//      rule D is the smallest rank whose exact discarded weight
+//      |A|_F^2 - sum_{kept} sigma_i^2 is within tolerance (this stays exact
+//      where FP32 cannot resolve the individual small sigma_i); the singular
+//      value rules apply the reference rule to these FP64 values.  The
+//      factors are V's rows and C's columns, so the output never has to be
+//      formed from A again.
 // The caller falls back to the FP64 split (svd_split_xfree) when the cluster
-// iteration did not converge, when a kept singular value lies below the FP32
-// resolution (1e-4 s_max), when a kept and a dropped direction are still
-// coupled by more than 1e-7 after the refinement (a cut gap below the FP32
-// backward error), or when the exact discarded weight breaks the strategy's
-// tolerance while fewer than max_bond_dimension values are kept.
+// iteration did not converge, when a resolved kept and a dropped direction
+// are still coupled by more than 1e-7 after the refinement (a cut gap below
+// the FP32 backward error), when a singular-value rule cuts below the FP32
+// resolution (1e-4 s_max), or when the exact discarded weight breaks the
+// strategy's tolerance while fewer than max_bond_dimension values are kept.
 // ---------------------------------------------------------------------------
 namespace {
 
 constexpr int kMixedMinRank = 24;  // smaller splits stay on the FP64 path
-constexpr int kMixedRefine = 3;    // refinement steps
+constexpr int kMixedRefine = 2;    // refinement steps
 constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
 constexpr double kMixedCutAngle = 1e-7;  // largest kept/dropped coupling accepted
+constexpr double kMixedMinTol = 1e-14;   // smallest relative-norm tolerance taken in mixed
 
 template <typename T>
 __global__ void k_gather_rows(const T* __restrict__ rows, int l, const int* __restrict__ perm,
@@ -1102,10 +1106,10 @@ __device__ __forceinline__ double re_of(cplx x) { return x.re; }
 
 // F = (I + E)^H from G and M (k x k, Hermitian), E as described above.
 // Pairs of rows that are both below FP32 resolution (lambda < blind2 *
-// lambda_0; row 0 has the largest norm) are left alone (E = 0): their FP32
-// directions are rounding noise, a first-order correction between them is
-// meaningless and would break their orthogonality; they are still decoupled
-// from the resolved rows.
+// lambda_0; row 0 has the largest norm) are only re-orthonormalised
+// (E = R / 2): their FP32 directions are rounding noise and a first-order
+// rotation between them is meaningless; they are still decoupled from the
+// resolved rows.
 template <typename T>
 __global__ void k_refine_matrix(const T* __restrict__ G, const T* __restrict__ M, int k,
                                 double blind2, T* __restrict__ F) {
@@ -1123,7 +1127,7 @@ __global__ void k_refine_matrix(const T* __restrict__ G, const T* __restrict__ M
     if (i == j) {
       Eji = S<T>::from_real(0.5 * (1.0 - mii));
     } else if (li < blind2 * lmax && lj < blind2 * lmax) {
-      Eji = S<T>::zero();
+      Eji = S<T>::scale(S<T>::neg(M[(size_t)j * k + i]), 0.5);
     } else {
       const T r = S<T>::neg(M[(size_t)j * k + i]);  // R_ji = -M_ji
       const T num = G[(size_t)j * k + i] + S<T>::scale(r, li);
@@ -1160,6 +1164,30 @@ __global__ void k_col_norms(const T* __restrict__ C, int rows, int cols, double*
 }
 
 // Exact discarded weight |A|^2 - sum_{j<D} s_j^2 into the split result.
+// Relative-norm-squared rule on exact weights: D = the smallest rank whose
+// discarded weight |A|^2 - sum_{j<D} s_j^2 (exact: s_j^2 are Rayleigh
+// quotients of orthonormal rows, |A|^2 was summed in FP64 from A itself) is at
+// most tol |A|^2, then clamped to max_bond_dimension (cython/truncation.pxi:
+// 251-287 states the same contract through the sorted singular values).
+// Overrides the rank the sorted-value rule gave; one thread.
+__global__ void k_exact_weight_rank(SplitResult* res, const double* __restrict__ s, int cnt,
+                                    sm_strategy st, const double* info) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double total = info[0];
+  const double allowed = st.tolerance * total;
+  double kept = 0.0;
+  int D = cnt;
+  for (int j = 0; j < cnt; ++j) {
+    kept += s[j] * s[j];
+    if (total - kept <= allowed) {
+      D = j + 1;
+      break;
+    }
+  }
+  D = max(1, min(D, st.max_bond_dimension));
+  res->D = D;
+}
+
 // Also info[2] = s[0], info[3] = s[D-1] for the host's checks.
 __global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, double* info) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -1174,15 +1202,21 @@ __global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, doub
 // row i and a dropped row j after the refinement (G = C^H C of the final rows,
 // lambda = s^2 in sorted order): the a-posteriori check that the kept
 // subspace is resolved to FP64 accuracy.  Writes info[4].
+// Pairs whose both values lie below the FP32 resolution (s < blind s_0) are
+// skipped: which of two unresolved directions is kept does not matter once
+// the kept weight is exact (the rank comes from the exact discarded weight).
 template <typename T>
 __global__ void k_cut_check(const T* __restrict__ G, int cnt, const int* __restrict__ perm,
-                            const double* __restrict__ s, const SplitResult* res, double* info) {
+                            const double* __restrict__ s, const SplitResult* res, double blind,
+                            double* info) {
   __shared__ double red[256];
   const int D = res->D;
+  const double sb = blind * s[0];
   double worst = 0.0;
   const long pairs = (long)D * (cnt - D);
   for (long e = threadIdx.x; e < pairs; e += blockDim.x) {
     const int a = (int)(e / (cnt - D)), b = D + (int)(e % (cnt - D));
+    if (s[a] < sb && s[b] < sb) continue;
     const double gap = s[a] * s[a] - s[b] * s[b];
     const double g = sqrt(S<T>::abs2(G[(size_t)perm[a] * cnt + perm[b]]));
     const double th = gap > 0.0 ? g / gap : (g > 0.0 ? 1e300 : 0.0);
@@ -1253,6 +1287,14 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   if (k < kMixedMinRank || strat.method == SM_DO_NOT_TRUNCATE || strat.tolerance <= 0.0)
     return SM_OK;
   if (!split_cluster_fits<T>(kw, l)) return SM_OK;
+  // the exact-weight rank rule resolves discarded weights down to the FP64
+  // rounding of |A|^2 - kept (~ k eps |A|^2): tighter relative tolerances
+  // take the FP64 path (counted as a fallback)
+  if (strat.method == SM_RELATIVE_NORM_SQUARED_ERROR && strat.tolerance < kMixedMinTol) {
+    ctx.stats.mixed_splits += 1;
+    ctx.stats.mixed_fallbacks += 1;
+    return SM_OK;
+  }
   const int kcap = k + 32;  // the Jacobi writes 32 blocks of ceil(rows / 32)
   T *rows, *V0, *V1, *Cb, *Gb, *Mb, *Fb;
   double *nrm, *s_sorted, *errors, *info, *cn;
@@ -1281,22 +1323,37 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
   struct Head {
     JacobiCtl c;
-    double info[2];
+    double info[7];
   };
+  // FP32 singular values: sorted, and the rank the rule gives on them; for the
+  // singular-value rules a cut below the FP32 resolution sends the split to
+  // the FP64 path right away
+  const size_t sort_smem = sizeof(unsigned long long) * (size_t)kcap;
+  if (sort_smem > 48 * 1024)
+    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sort_smem));
+  k_sort_truncate<<<1, 1024, sort_smem, st>>>(nrm, kcap, strat, perm, s_sorted, errors, ctl, res);
+  note_launch();
+  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
   Head* h = reinterpret_cast<Head*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(&h->c, ctl, sizeof(JacobiCtl), cudaMemcpyDeviceToHost, st));
-  SM_CUDA_CHECK(cudaMemcpyAsync(h->info, info, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaMemcpyAsync(h->info, info, 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
   const double norm2 = h->info[0];  // the pinned block is reused below
   const JacobiCtl hc = h->c;
   ctx.stats.mixed_splits += 1;
+  ctx.stats.cluster_qr_ms += h->info[5];
+  ctx.stats.cluster_jacobi_ms += h->info[6];
   if (ctx.timing) {
     float ms = 0.f;
     SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
     ctx.stats.cluster_ms += ms;
   }
   ctx.stats.jacobi_sweeps += hc.sweeps;
-  if (hc.status != 0) {
+  const bool exact_rule = strat.method == SM_RELATIVE_NORM_SQUARED_ERROR;
+  if (hc.status != 0 || (!exact_rule && h->info[3] < kMixedBlind * h->info[2])) {
     ctx.stats.mixed_fallbacks += 1;
     return SM_OK;
   }
@@ -1309,13 +1366,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(ctx.scratch("mx.M", (size_t)cnt * cnt, &Mb));
   SM_CHECK(ctx.scratch("mx.F", (size_t)cnt * cnt, &Fb));
   SM_CHECK(ctx.scratch("mx.cn", (size_t)cnt, &cn));
-  // rows by decreasing norm, normalised
-  const size_t sort_smem = sizeof(unsigned long long) * (size_t)kcap;
-  if (sort_smem > 48 * 1024)
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sort_smem));
-  k_sort_truncate<<<1, 1024, sort_smem, st>>>(nrm, kcap, strat, perm, s_sorted, errors, ctl, res);
-  note_launch();
+  // rows by decreasing norm (sorted above), normalised
   k_gather_rows<T><<<grid_for((size_t)cnt * l), 256, 0, st>>>(rows, l, perm, s_sorted, cnt, V0);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
@@ -1347,7 +1398,8 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_N, cnt, l, cnt, one, Fb, cnt, V, l, zero, Vn, l));
     std::swap(V, Vn);
   }
-  // Newton-Schulz: orthonormality error e -> 1.5 e^2
+  // Newton-Schulz: the refinement leaves the orthonormality error of nearly
+  // degenerate pairs at ~1e-11; one step takes it to 1.5 e^2
   SM_CHECK(normalise(V));
   SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, cnt, cnt, l, one, V, l, V, l, zero, Mb, cnt));
   k_ns_matrix<T><<<grid_for((size_t)cnt * cnt), 256, 0, st>>>(Mb, cnt, Fb);
@@ -1363,10 +1415,14 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   const size_t smem2 = sizeof(unsigned long long) * (size_t)cnt;
   k_sort_truncate<<<1, 1024, smem2, st>>>(cn, cnt, strat, perm, s_sorted, errors, ctl, res);
   note_launch();
+  if (exact_rule) {
+    k_exact_weight_rank<<<1, 1, 0, st>>>(res, s_sorted, cnt, strat, info);
+    note_launch();
+  }
   k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info);
   note_launch();
   SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
-  k_cut_check<T><<<1, 256, 0, st>>>(Gb, cnt, perm, s_sorted, res, info);
+  k_cut_check<T><<<1, 256, 0, st>>>(Gb, cnt, perm, s_sorted, res, kMixedBlind, info);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   SplitResult* hr = reinterpret_cast<SplitResult*>(ctx.pinned);
@@ -1383,7 +1439,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // kept, sends the split to the FP64 path.
   const double s_last = hs[1];
   const double cut_angle = hs[2];
-  if (s_last < kMixedBlind * s0 || !(cut_angle <= kMixedCutAngle) ||
+  if ((!exact_rule && s_last < kMixedBlind * s0) || !(cut_angle <= kMixedCutAngle) ||
       (D < strat.max_bond_dimension && D < k &&
        r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12))) {
     ctx.stats.mixed_fallbacks += 1;

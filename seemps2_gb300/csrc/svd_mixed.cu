@@ -13,17 +13,19 @@
 //            for operators with 1/h^2 ~ 1e18 entries).
 //   phase 1  Householder QR of W (reflectors act on the columns, length kw),
 //            one cluster barrier per step; the warp that owns column j + 1
-//            forms the next reflector in the same step.  The factorisation
-//            stops once the trailing block holds at most `thr_rel` of
-//            |W|_F^2 (rank revealing), leaving keff rows of R.
-//   phase 2  every warp of the cluster gathers two rows of R (upper
-//            trapezoidal, keff x l) into registers.
-//   phase 3  one-sided Jacobi on the rows of R in the circle ordering: warp w
-//            holds the rows at positions w and n-1-w, rotates them, then
-//            passes its rows to the neighbouring warps through DSMEM
-//            mailboxes (double-buffered by round parity) and meets the
-//            cluster barrier.  A round costs one barrier plus the mailbox
-//            stores; no row ever goes through L2.
+//            forms the next reflector in the same step and its CTA pushes it
+//            into every other CTA before the barrier (no read after the
+//            barrier leaves the SM).  The factorisation stops once the
+//            trailing block holds at most thr of |W|_F^2 (rank revealing),
+//            leaving keff rows of R.
+//   phase 2  the rows of R are cut into 32 blocks of r = ceil(keff / 32) rows;
+//            CTA c holds block positions c and 31 - c in shared memory.
+//   phase 3  block-cyclic one-sided Jacobi: per sweep, the pairs inside each
+//            block once, then 31 block rounds in which each CTA rotates all
+//            r x r pairs between its two blocks (r local rounds of r disjoint
+//            pairs, one warp per pair, CTA barriers only) and passes its
+//            blocks to the neighbouring CTAs through double-buffered DSMEM
+//            mailboxes.  One cluster barrier per block round (31 per sweep).
 //   phase 4  the rows (= diag(s) V^H of the rows of R, i.e. of W) go back to
 //            global memory in FP64, rescaled by |W|_F, with their FP64 norms.
 //
@@ -119,12 +121,18 @@ __device__ __forceinline__ double warp_sum(double x) {
 // Control words of one CTA (after the data region of its shared memory).
 struct CtrlS {
   int flag[2];        // CTA 0: a rotation happened in the sweep of this parity
-  float tau[2];       // reflector tau, by step parity
-  float part[2][kCW]; // CTA 0: trailing-weight partials by step parity
-  double part64[kCW]; // CTA 0: |W|^2 partials
+  float tau[2];       // reflector tau, by step parity (pushed by the owner)
+  float part[2][kCW]; // trailing-weight partials of all CTAs, by step parity
+  double part64[kCW]; // |W|^2 partials of all CTAs
   float red[kCNW];    // CTA-local reduction scratch
   double red64[kCNW];
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // Shared memory (bytes) for a k_split_cluster launch.
 template <typename T, int E>
@@ -168,6 +176,7 @@ __global__ void __launch_bounds__(kCNT, 1)
   };
 
   // ---- phase 0: |W|^2 (FP64) and the scaled FP32 copy ------------------------
+  const unsigned long long t_start = global_ns();
   if (tid < 2) ctrl->flag[tid] = 0;
   {
     double acc = 0.0;
@@ -179,15 +188,15 @@ __global__ void __launch_bounds__(kCNT, 1)
     acc = warp_sum(acc);
     if (lane == 0) ctrl->red64[warp] = acc;
     __syncthreads();
-    if (tid == 0) {
+    if (tid < kCW) {  // every CTA receives every partial
       double t = 0.0;
       for (int w = 0; w < kCNW; ++w) t += ctrl->red64[w];
-      ctrl0->part64[rank] = t;
+      cluster.map_shared_rank(ctrl, tid)->part64[rank] = t;
     }
   }
   cluster.sync();
   double norm2 = 0.0;
-  for (int r = 0; r < kCW; ++r) norm2 += ctrl0->part64[r];
+  for (int r = 0; r < kCW; ++r) norm2 += ctrl->part64[r];
   const double nrm = sqrt(norm2);
   const double scale = nrm > 0.0 ? 1.0 / nrm : 1.0;
   // stop once the trailing block holds at most max(thr_rel |W|^2, thr_abs)
@@ -223,25 +232,34 @@ __global__ void __launch_bounds__(kCNT, 1)
       col[j] = d;
     }
   };
+  // The owner CTA of the next reflector pushes it (and tau) into every other
+  // CTA's buffer of that parity before the barrier; the trailing-weight
+  // partials are pushed to every CTA the same way, so after the barrier all
+  // reads are local.
+  auto push_reflector = [&](int j, int par) {  // all threads of the owner CTA
+    const F* v = refl + (size_t)par * kw;
+    const int cnt = kw - j;
+    for (int e = tid; e < cnt * (kCW - 1); e += kCNT) {
+      const int dst = e / cnt, i = j + e % cnt;
+      const int r = dst < rank ? dst : dst + 1;
+      cluster.map_shared_rank(refl + (size_t)par * kw, r)[i] = v[i];
+    }
+    if (tid < kCW && tid != rank) cluster.map_shared_rank(ctrl, tid)->tau[par] = ctrl->tau[par];
+  };
   if (rank == 0 && warp == 0 && l > 0) {
     float xn2 = 0.f;
     for (int i = lane; i < kw; i += 32) xn2 += f_abs2(cols[i]);
     xn2 = warp_sum(xn2);
     make_reflector(cols, 0, xn2, refl, &ctrl->tau[0]);
   }
+  __syncthreads();
+  if (rank == 0 && l > 0) push_reflector(0, 0);
   cluster.sync();
   int keff = kmax;
   float trail = 0.f;
   for (int j = 0; j < kmax; ++j) {
     const int par = j & 1;
-    const int owner = j % kCW;
-    F* v = refl + (size_t)par * kw;
-    if (rank != owner) {
-      const F* vr = cluster.map_shared_rank(v, owner);
-      for (int i = j + tid; i < kw; i += kCNT) v[i] = vr[i];
-      if (tid == 0) ctrl->tau[par] = cluster.map_shared_rank(ctrl, owner)->tau[par];
-    }
-    __syncthreads();
+    const F* v = refl + (size_t)par * kw;
     const float tau = ctrl->tau[par];
     float tw = 0.f;  // this warp's trailing weight
     for (int s = warp; s < ncs; s += kCNW) {
@@ -270,20 +288,22 @@ __global__ void __launch_bounds__(kCNT, 1)
     }
     if (lane == 0) ctrl->red[warp] = tw;
     __syncthreads();
-    if (tid == 0) {
+    if (j + 1 < kmax && rank == (j + 1) % kCW) push_reflector(j + 1, par ^ 1);
+    if (tid < kCW) {
       float t = 0.f;
       for (int w = 0; w < kCNW; ++w) t += ctrl->red[w];
-      ctrl0->part[par][rank] = t;
+      cluster.map_shared_rank(ctrl, tid)->part[par][rank] = t;
     }
     cluster.sync();
     float t = 0.f;
-    for (int r = 0; r < kCW; ++r) t += ctrl0->part[par][r];
+    for (int r = 0; r < kCW; ++r) t += ctrl->part[par][r];
     trail = t;
     if (t <= thr) {
       keff = j + 1;
       break;
     }
   }
+  const unsigned long long t_qr = global_ns();
 
   // ---- phase 2: rows of R into the row blocks ---------------------------------
   // 32 block positions of r rows (zero rows past keff); CTA c holds position c
@@ -319,37 +339,69 @@ __global__ void __launch_bounds__(kCNT, 1)
   }
 
   // ---- phase 3: block-cyclic one-sided Jacobi ------------------------------
-  // Rotates rows p, q (shared memory, this warp); true if it rotated.
-  auto rotate_pair = [&](F* rp, F* rq) -> bool {
-    F u[E], v[E];
-    float a = 0.f, b = 0.f, gr = 0.f, gi = 0.f;
+  // A lane holds NV float4 of a row (elements 4 lane + 128 e .. + 3, natural
+  // order), loaded and stored as 128-bit shared-memory accesses.
+  constexpr int NV = (E * (int)sizeof(F)) / 16;
+  auto load_row = [&](const F* row, float4* x) {
+    const float4* r4 = reinterpret_cast<const float4*>(row);
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      u[e] = rp[lane + 32 * e];
-      v[e] = rq[lane + 32 * e];
-      a += f_abs2(u[e]);
-      b += f_abs2(v[e]);
-      f_dotc(u[e], v[e], gr, gi);
+    for (int e = 0; e < NV; ++e) x[e] = r4[lane + 32 * e];
+  };
+  auto store_row = [&](F* row, const float4* x) {
+    float4* r4 = reinterpret_cast<float4*>(row);
+#pragma unroll
+    for (int e = 0; e < NV; ++e) r4[lane + 32 * e] = x[e];
+  };
+  // Rotates the register rows u, v of this warp; true if it rotated.
+  auto rotate_regs = [&](float4* u, float4* v) -> bool {
+    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f, gr0 = 0.f, gr1 = 0.f, gi0 = 0.f, gi1 = 0.f;
+#pragma unroll
+    for (int e = 0; e < NV; ++e) {
+      const float4 p = u[e], q = v[e];
+      a0 = fmaf(p.x, p.x, fmaf(p.y, p.y, a0));
+      a1 = fmaf(p.z, p.z, fmaf(p.w, p.w, a1));
+      b0 = fmaf(q.x, q.x, fmaf(q.y, q.y, b0));
+      b1 = fmaf(q.z, q.z, fmaf(q.w, q.w, b1));
+      if constexpr (sizeof(F) == 4) {
+        gr0 = fmaf(p.x, q.x, fmaf(p.y, q.y, gr0));
+        gr1 = fmaf(p.z, q.z, fmaf(p.w, q.w, gr1));
+      } else {  // (x, y) and (z, w) are complex numbers: conj(p) q
+        gr0 = fmaf(p.x, q.x, fmaf(p.y, q.y, gr0));
+        gi0 = fmaf(p.x, q.y, fmaf(-p.y, q.x, gi0));
+        gr1 = fmaf(p.z, q.z, fmaf(p.w, q.w, gr1));
+        gi1 = fmaf(p.z, q.w, fmaf(-p.w, q.z, gi1));
+      }
     }
-    a = warp_sum(a);
-    b = warp_sum(b);
-    gr = warp_sum(gr);
-    gi = warp_sum(gi);
+    const float a = warp_sum(a0 + a1), b = warp_sum(b0 + b1), gr = warp_sum(gr0 + gr1);
+    float gi = 0.f;
+    if constexpr (sizeof(F) != 4) gi = warp_sum(gi0 + gi1);
     const float g2 = fmaf(gr, gr, gi * gi);
     if (!(g2 > 0.f && g2 > tol2 * a * b)) return false;
-    const float gabs = sqrtf(g2);
-    const float zeta = 0.5f * (b - a) / gabs;
+    const float rg = rsqrtf(g2);
+    const float zeta = 0.5f * (b - a) * rg;
     const float az = fabsf(zeta);
     const float tt =
-        copysignf(az < 1e18f ? 1.0f / (az + sqrtf(fmaf(az, az, 1.0f))) : 0.5f / az, zeta);
+        copysignf(az < 1e18f ? __frcp_rn(az + sqrtf(fmaf(az, az, 1.0f))) : 0.5f / az, zeta);
     const float c = rsqrtf(fmaf(tt, tt, 1.0f));
     const float sn = c * tt;
-    const float er = gr / gabs, ei = gi / gabs;
+    const float ar = sn * gr * rg, ai = sn * gi * rg;  // s e
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      f_rot(u[e], v[e], c, sn, er, ei);
-      rp[lane + 32 * e] = u[e];
-      rq[lane + 32 * e] = v[e];
+    for (int e = 0; e < NV; ++e) {
+      const float4 p = u[e], q = v[e];
+      float4 np, nq;
+      if constexpr (sizeof(F) == 4) {
+        np = make_float4(fmaf(c, p.x, -ar * q.x), fmaf(c, p.y, -ar * q.y), fmaf(c, p.z, -ar * q.z),
+                         fmaf(c, p.w, -ar * q.w));
+        nq = make_float4(fmaf(ar, p.x, c * q.x), fmaf(ar, p.y, c * q.y), fmaf(ar, p.z, c * q.z),
+                         fmaf(ar, p.w, c * q.w));
+      } else {  // p' = c p - conj(s e) q ; q' = (s e) p + c q
+        np = make_float4(c * p.x - (ar * q.x + ai * q.y), c * p.y - (ar * q.y - ai * q.x),
+                         c * p.z - (ar * q.z + ai * q.w), c * p.w - (ar * q.w - ai * q.z));
+        nq = make_float4((ar * p.x - ai * p.y) + c * q.x, (ar * p.y + ai * p.x) + c * q.y,
+                         (ar * p.z - ai * p.w) + c * q.z, (ar * p.w + ai * p.z) + c * q.w);
+      }
+      u[e] = np;
+      v[e] = nq;
     }
     return true;
   };
@@ -370,23 +422,49 @@ __global__ void __launch_bounds__(kCNT, 1)
           else { p = (t + w8) % (rp2 - 1); q = (t + rp2 - 1 - w8) % (rp2 - 1); }
           if (p < r && q < r) {
             F* base = side ? Bb : Tb;
-            if (rotate_pair(base + (size_t)p * LP, base + (size_t)q * LP)) mark(sweep);
+            float4 u[NV], v[NV];
+            load_row(base + (size_t)p * LP, u);
+            load_row(base + (size_t)q * LP, v);
+            if (rotate_regs(u, v)) {
+              store_row(base + (size_t)p * LP, u);
+              store_row(base + (size_t)q * LP, v);
+              mark(sweep);
+            }
           }
         }
         __syncthreads();
       }
     }
-    // 31 block rounds: top x bottom pairs, then the blocks move
+    // 31 block rounds: top x bottom pairs (warp w keeps top row w in
+    // registers, the bottom rows come by), then the blocks move
     for (int br = 0; br < 2 * kCW - 1; ++br) {
+      float4 tr[NV];
+      if (warp < r) load_row(Tb + (size_t)warp * LP, tr);
+      bool trot = false;
       for (int t = 0; t < r; ++t) {
-        if (warp < r && rotate_pair(Tb + (size_t)warp * LP, Bb + (size_t)((warp + t) % r) * LP))
-          mark(sweep);
+        if (warp < r) {
+          F* brow = Bb + (size_t)((warp + t) % r) * LP;
+          float4 v[NV];
+          load_row(brow, v);
+          if (rotate_regs(tr, v)) {
+            store_row(brow, v);
+            trot = true;
+          }
+        }
         __syncthreads();
       }
+      if (trot) {
+        store_row(Tb + (size_t)warp * LP, tr);
+        mark(sweep);
+      }
+      __syncthreads();
       const int par = br & 1;
+      const int n4 = blk * (int)sizeof(F) / 16;
       auto send = [&](const F* src, int dst_rank, int slot) {
-        F* d = cluster.map_shared_rank(mbox + (size_t)(slot * 2 + par) * blk, dst_rank);
-        for (int f = tid; f < blk; f += kCNT) d[f] = src[f];
+        float4* d = reinterpret_cast<float4*>(
+            cluster.map_shared_rank(mbox + (size_t)(slot * 2 + par) * blk, dst_rank));
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        for (int f = tid; f < n4; f += kCNT) d[f] = s4[f];
       };
       if (rank == 0) send(Bb, 1, 0);
       else {
@@ -394,18 +472,20 @@ __global__ void __launch_bounds__(kCNT, 1)
         send(Bb, rank - 1, 1);
       }
       cluster.sync();
-      const F* mt = mbox + (size_t)(0 * 2 + par) * blk;
-      const F* mb = mbox + (size_t)(1 * 2 + par) * blk;
+      const float4* mt = reinterpret_cast<const float4*>(mbox + (size_t)(0 * 2 + par) * blk);
+      const float4* mb = reinterpret_cast<const float4*>(mbox + (size_t)(1 * 2 + par) * blk);
+      float4* T4 = reinterpret_cast<float4*>(Tb);
+      float4* B4 = reinterpret_cast<float4*>(Bb);
       if (rank == kCW - 1) {
-        for (int f = tid; f < blk; f += kCNT) Bb[f] = Tb[f];
+        for (int f = tid; f < n4; f += kCNT) B4[f] = T4[f];
         __syncthreads();
-        for (int f = tid; f < blk; f += kCNT) Tb[f] = mt[f];
+        for (int f = tid; f < n4; f += kCNT) T4[f] = mt[f];
       } else if (rank == 0) {
-        for (int f = tid; f < blk; f += kCNT) Bb[f] = mb[f];
+        for (int f = tid; f < n4; f += kCNT) B4[f] = mb[f];
       } else {
-        for (int f = tid; f < blk; f += kCNT) {
-          Tb[f] = mt[f];
-          Bb[f] = mb[f];
+        for (int f = tid; f < n4; f += kCNT) {
+          T4[f] = mt[f];
+          B4[f] = mb[f];
         }
       }
       __syncthreads();
@@ -449,6 +529,8 @@ __global__ void __launch_bounds__(kCNT, 1)
     ctl_out->nact = keff;
     info[0] = norm2;
     info[1] = (double)trail * norm2;
+    info[5] = 1e-6 * (double)(t_qr - t_start);       // ms: load + QR
+    info[6] = 1e-6 * (double)(global_ns() - t_qr);   // ms: gather + Jacobi + store
   }
   cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
@@ -514,9 +596,9 @@ int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw
   return SM_OK;
 }
 
+// Elements per lane of a row (a multiple of 4: rows move as float4).
 inline int e_bucket(int l) {
   const int need = (l + 31) / 32;
-  if (need <= 2) return 2;
   if (need <= 4) return 4;
   if (need <= 8) return 8;
   if (need <= 12) return 12;
@@ -537,7 +619,6 @@ bool split_cluster_fits(int kw, int l) {
   // the sizes beyond the shared-memory amount, which is re-checked below.
   size_t smem = 0;
   switch (e) {
-    case 2: return cluster_config<T, 2>(kw, l, &smem);
     case 4: return cluster_config<T, 4>(kw, l, &smem);
     case 8: return cluster_config<T, 8>(kw, l, &smem);
     case 12: return cluster_config<T, 12>(kw, l, &smem);
@@ -559,7 +640,6 @@ int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, do
   case EV:                                                                                    \
     return launch_split_cluster<T, EV>(st, A, n, trans, kw, l, thr_rel, thr_abs, max_sweeps, \
                                        out_rows, out_nrm, kcap, ctl, info)
-    SM_C(2);
     SM_C(4);
     SM_C(8);
     SM_C(12);

@@ -109,15 +109,16 @@ def test_mixed_split_against_oracle(mixed, cplx, case, side):
     D = L.shape[-1]
     stats = _lib.stats_read()
     assert stats["mixed_splits"] >= 1
-    # "tolerance_cut" cuts below 1e-4 s_max, beyond the FP32 stage: FP64 path
-    if case == "tolerance_cut":
-        assert stats["mixed_fallbacks"] == 1
+    # "tolerance_cut" cuts below 1e-4 s_max, beyond the FP32 stage's resolution of
+    # individual values: the rank comes from the exact discarded weight instead
+    # (never below the oracle's, a few above at most, weight within tolerance)
     norm2 = np.linalg.norm(A) ** 2
     # the kept rank: identical where the spectrum separates it
     if case == "gap_at_max_bond":
         assert D == oL.shape[-1] == 256
     else:
-        assert abs(D - oL.shape[-1]) <= 1
+        assert oL.shape[-1] <= D <= oL.shape[-1] + 3
+        assert err**2 <= 1e-12 * norm2 * (1 + 1e-9)
     # isometry of the orthogonal factor to FP64 rounding
     if side == "left":
         M = L.reshape(-1, D)
