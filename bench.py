@@ -421,6 +421,8 @@ def main():
                 "cluster_ms_per_step": stt["cluster_ms"],
                 "cluster_qr_ms_per_step": timed_stats["cluster_qr_ms"] / k,
                 "cluster_jacobi_ms_per_step": timed_stats["cluster_jacobi_ms"] / k,
+                "fallbacks_coupling_per_step": timed_stats["mixed_fallback_cut"] / k,
+                "fallbacks_fp32_per_step": timed_stats["mixed_fallback_fp32"] / k,
             }
         print(json.dumps(line), flush=True)
     if dist:

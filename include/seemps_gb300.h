@@ -238,6 +238,8 @@ typedef struct sm_stats {
   double cluster_ms;       /* event-timed device time of the cluster kernel */
   double cluster_qr_ms;    /* of which: load + FP32 QR (device timer) */
   double cluster_jacobi_ms;/* of which: FP32 Jacobi + store (device timer) */
+  int64_t mixed_fallback_cut;  /* fallbacks: kept/dropped coupling left after refinement */
+  int64_t mixed_fallback_fp32; /* fallbacks: FP32 stage (convergence, resolution, weight) */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

@@ -66,6 +66,8 @@ class sm_stats(C.Structure):
         ("cluster_ms", C.c_double),
         ("cluster_qr_ms", C.c_double),
         ("cluster_jacobi_ms", C.c_double),
+        ("mixed_fallback_cut", C.c_int64),
+        ("mixed_fallback_fp32", C.c_int64),
     ]
 
 

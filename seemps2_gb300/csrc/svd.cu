@@ -1064,9 +1064,9 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
 //      factors are V's rows and C's columns, so the output never has to be
 //      formed from A again.
 // The caller falls back to the FP64 split (svd_split_xfree) when the cluster
-// iteration did not converge, when a resolved kept and a dropped direction
-// are still coupled by more than 1e-7 after the refinement (a cut gap below
-// the FP32 backward error), when a singular-value rule cuts below the FP32
+// iteration did not converge, when the coupling left between a resolved kept
+// and a dropped direction after the refinement could move the truncated
+// matrix by more than 1e-6 |A|_F (a cut gap below the FP32 backward error), when a singular-value rule cuts below the FP32
 // resolution (1e-4 s_max), or when the exact discarded weight breaks the
 // strategy's tolerance while fewer than max_bond_dimension values are kept.
 // ---------------------------------------------------------------------------
@@ -1075,7 +1075,7 @@ namespace {
 constexpr int kMixedMinRank = 24;  // smaller splits stay on the FP64 path
 constexpr int kMixedRefine = 2;    // refinement steps
 constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
-constexpr double kMixedCutAngle = 1e-7;  // largest kept/dropped coupling accepted
+constexpr double kMixedCutAmp = 1e-6;  // largest kept/dropped coupling (angle s_i / |A|)
 constexpr double kMixedMinTol = 1e-14;   // smallest relative-norm tolerance taken in mixed
 
 template <typename T>
@@ -1198,10 +1198,12 @@ __global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, doub
   info[3] = s[max(res->D, 1) - 1];
 }
 
-// Largest coupling angle |G_ij| / (lambda_i - lambda_j) left between a kept
-// row i and a dropped row j after the refinement (G = C^H C of the final rows,
-// lambda = s^2 in sorted order): the a-posteriori check that the kept
-// subspace is resolved to FP64 accuracy.  Writes info[4].
+// Largest state change left by the coupling between a kept row i and a
+// dropped row j after the refinement: the angle |G_ij| / (lambda_i - lambda_j)
+// (G = C^H C of the final rows, lambda = s^2 in sorted order) moves the
+// truncated matrix by about angle * s_i, so the check takes
+// max angle * s_i / |A|_F; its square bounds the fidelity error the split can
+// add.  Writes info[4].
 // Pairs whose both values lie below the FP32 resolution (s < blind s_0) are
 // skipped: which of two unresolved directions is kept does not matter once
 // the kept weight is exact (the rank comes from the exact discarded weight).
@@ -1212,6 +1214,7 @@ __global__ void k_cut_check(const T* __restrict__ G, int cnt, const int* __restr
   __shared__ double red[256];
   const int D = res->D;
   const double sb = blind * s[0];
+  const double rnorm = info[0] > 0.0 ? 1.0 / sqrt(info[0]) : 0.0;
   double worst = 0.0;
   const long pairs = (long)D * (cnt - D);
   for (long e = threadIdx.x; e < pairs; e += blockDim.x) {
@@ -1220,7 +1223,7 @@ __global__ void k_cut_check(const T* __restrict__ G, int cnt, const int* __restr
     const double gap = s[a] * s[a] - s[b] * s[b];
     const double g = sqrt(S<T>::abs2(G[(size_t)perm[a] * cnt + perm[b]]));
     const double th = gap > 0.0 ? g / gap : (g > 0.0 ? 1e300 : 0.0);
-    worst = fmax(worst, th);
+    worst = fmax(worst, th * s[a] * rnorm);
   }
   red[threadIdx.x] = worst;
   __syncthreads();
@@ -1355,6 +1358,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   const bool exact_rule = strat.method == SM_RELATIVE_NORM_SQUARED_ERROR;
   if (hc.status != 0 || (!exact_rule && h->info[3] < kMixedBlind * h->info[2])) {
     ctx.stats.mixed_fallbacks += 1;
+    ctx.stats.mixed_fallback_fp32 += 1;
     return SM_OK;
   }
   const int cnt = std::max(1, std::min(hc.nact, k));
@@ -1439,10 +1443,14 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // kept, sends the split to the FP64 path.
   const double s_last = hs[1];
   const double cut_angle = hs[2];
-  if ((!exact_rule && s_last < kMixedBlind * s0) || !(cut_angle <= kMixedCutAngle) ||
-      (D < strat.max_bond_dimension && D < k &&
-       r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12))) {
+  const bool blind = !exact_rule && s_last < kMixedBlind * s0;
+  const bool coupled = !(cut_angle <= kMixedCutAmp);
+  const bool over = D < strat.max_bond_dimension && D < k &&
+                    r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
+  if (blind || coupled || over) {
     ctx.stats.mixed_fallbacks += 1;
+    if (coupled) ctx.stats.mixed_fallback_cut += 1;
+    else ctx.stats.mixed_fallback_fp32 += 1;
     return SM_OK;
   }
   T* iso = want_u ? left : right;

@@ -237,12 +237,11 @@ __global__ void __launch_bounds__(kCNT, 1)
   // partials are pushed to every CTA the same way, so after the barrier all
   // reads are local.
   auto push_reflector = [&](int j, int par) {  // all threads of the owner CTA
-    const F* v = refl + (size_t)par * kw;
-    const int cnt = kw - j;
-    for (int e = tid; e < cnt * (kCW - 1); e += kCNT) {
-      const int dst = e / cnt, i = j + e % cnt;
-      const int r = dst < rank ? dst : dst + 1;
-      cluster.map_shared_rank(refl + (size_t)par * kw, r)[i] = v[i];
+    F* v = refl + (size_t)par * kw;
+    for (int r = 0; r < kCW; ++r) {
+      if (r == rank) continue;
+      F* d = cluster.map_shared_rank(v, r);
+      for (int i = j + tid; i < kw; i += kCNT) d[i] = v[i];
     }
     if (tid < kCW && tid != rank) cluster.map_shared_rank(ctrl, tid)->tau[par] = ctrl->tau[par];
   };
