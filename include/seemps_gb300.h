@@ -99,8 +99,40 @@ int sm_ctx_destroy(void* ctx);
  *                      when it exceeds the strategy's tolerance with fewer
  *                      than max_bond_dimension values kept.  Ranks may differ
  *                      from the reference's at the tolerance boundary. */
-enum { SM_PRECISION_FP64 = 0, SM_PRECISION_MIXED = 1 };
+enum { SM_PRECISION_FP64 = 0, SM_PRECISION_MIXED = 1, SM_PRECISION_MIXED_LEARNED = 2 };
+/* SM_PRECISION_MIXED_LEARNED: as SM_PRECISION_MIXED, but the rank predictor set
+ * with sm_rank_model_set predicts each split's kept rank r and a randomized
+ * range finder (an FP64 GEMM with a fixed Gaussian sketch of r + 10 rows)
+ * replaces the FP32 rank-revealing QR; the exact discarded-weight check sends
+ * a split whose sketch missed weight to the FP64 Jacobi SVD. */
 int sm_ctx_set_precision(void* ctx, int precision);
+
+/* ---- rank predictor (no reference counterpart) ------------------------------
+ * An MLP with GELU hidden layers; parameters are one FP32 device array, layer
+ * by layer W_k (dims[k+1] x dims[k], row-major) then b_k (dims[k+1]).  The
+ * forward / backward / MSE / Adam entry points train it on the GPU; features
+ * of every split can be recorded (sm_rank_features_record) together with the
+ * kept rank; sm_rank_model_set installs a trained model (dims[0] =
+ * SM_RANK_FEATURES, one output = log2 of the kept rank) for
+ * SM_PRECISION_MIXED_LEARNED.  Features of a split: log10(s_i / s_0) of the 32
+ * largest singular values of the previous split (-20 padding), site / n,
+ * log10(tolerance), log2(1 + previous kept rank), log2(min(m, n)),
+ * log2(bond cap). */
+#define SM_RANK_FEATURES 37
+int64_t sm_mlp_param_count(int n_layers, const int* dims);
+int64_t sm_mlp_cache_count(int n_layers, const int* dims, int batch);
+int sm_mlp_forward(void* ctx, int n_layers, const int* dims, const float* params, const float* X,
+                   int batch, float* Y, float* cache, void* stream);
+int sm_mlp_backward(void* ctx, int n_layers, const int* dims, const float* params, const float* X,
+                    int batch, const float* cache, const float* dY, float* grads, void* stream);
+int sm_mse_loss(void* ctx, const float* yhat, const float* y, int batch, float* dyhat, float* loss,
+                void* stream);
+int sm_adam_step(void* ctx, float* p, const float* g, float* m, float* v, int64_t n, float lr,
+                 float beta1, float beta2, float eps, int step, void* stream);
+int sm_rank_model_set(void* ctx, int n_layers, const int* dims, const float* params);
+int sm_rank_features_record(void* ctx, int on);
+int sm_rank_features_read(void* ctx, float* X, int* D, int cap, int* count);
+int sm_rank_predict(void* ctx, const float* X, int batch, float* out, void* stream);
 
 /* Kernel-level entry of the mixed split's FP32 stage (no reference
  * counterpart; for unit tests of that stage): rank-revealing QR + one-sided
@@ -240,6 +272,9 @@ typedef struct sm_stats {
   double cluster_jacobi_ms;/* of which: FP32 Jacobi + store (device timer) */
   int64_t mixed_fallback_cut;  /* fallbacks: kept/dropped coupling left after refinement */
   int64_t mixed_fallback_fp32; /* fallbacks: FP32 stage (convergence, resolution, weight) */
+  int64_t mixed_sketched;      /* mixed splits that used the predicted-rank sketch */
+  int64_t mixed_fallback_sketch; /* fallbacks: the sketch missed weight */
+  int64_t rank_predicted_sum;  /* predicted kept ranks, summed */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

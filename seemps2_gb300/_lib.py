@@ -68,6 +68,9 @@ class sm_stats(C.Structure):
         ("cluster_jacobi_ms", C.c_double),
         ("mixed_fallback_cut", C.c_int64),
         ("mixed_fallback_fp32", C.c_int64),
+        ("mixed_sketched", C.c_int64),
+        ("mixed_fallback_sketch", C.c_int64),
+        ("rank_predicted_sum", C.c_int64),
     ]
 
 
@@ -113,7 +116,21 @@ SIGNATURES = {
     "sm_stats_reset": (C.c_int, [vp, C.c_int]),
     "sm_stats_read": (C.c_int, [vp, C.POINTER(sm_stats)]),
     "sm_probe_fp64": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, vp]),
+    # rank predictor (device pointers as void*, dims as a host int array)
+    "sm_mlp_param_count": (C.c_int64, [C.c_int, ip]),
+    "sm_mlp_cache_count": (C.c_int64, [C.c_int, ip, C.c_int]),
+    "sm_mlp_forward": (C.c_int, [vp, C.c_int, ip, vp, vp, C.c_int, vp, vp, vp]),
+    "sm_mlp_backward": (C.c_int, [vp, C.c_int, ip, vp, vp, C.c_int, vp, vp, vp, vp]),
+    "sm_mse_loss": (C.c_int, [vp, vp, vp, C.c_int, vp, vp, vp]),
+    "sm_adam_step": (C.c_int, [vp, vp, vp, vp, vp, C.c_int64, C.c_float, C.c_float, C.c_float,
+                               C.c_float, C.c_int, vp]),
+    "sm_rank_model_set": (C.c_int, [vp, C.c_int, ip, vp]),
+    "sm_rank_features_record": (C.c_int, [vp, C.c_int]),
+    "sm_rank_features_read": (C.c_int, [vp, vp, vp, C.c_int, ip]),
+    "sm_rank_predict": (C.c_int, [vp, vp, C.c_int, vp, vp]),
 }
+
+RANK_FEATURES = 37
 
 _lib = None
 _lock = threading.Lock()
@@ -238,12 +255,13 @@ class SplitTrace:
         return False
 
 
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "mixed+learned": 2}
 
 
 def set_precision(mode: str, device: int = 0) -> None:
-    """Arithmetic of the SVD splits: "fp64" (default, reference ranks) or
-    "mixed" (FP32 cluster factorisation refined by FP64 GEMMs)."""
+    """Arithmetic of the SVD splits: "fp64" (default, reference ranks), "mixed"
+    (FP32 cluster factorisation refined by FP64 GEMMs) or "mixed+learned" (as
+    "mixed", with the installed rank predictor sizing a randomized sketch)."""
     if mode not in PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {mode!r}")
     check(load().sm_ctx_set_precision(context(device), PRECISIONS[mode]))

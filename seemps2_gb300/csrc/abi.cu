@@ -184,7 +184,8 @@ int sm_ctx_destroy(void* ctx) {
 
 int sm_ctx_set_precision(void* ctx, int precision) {
   SM_GUARD_CTX(ctx);
-  if (precision != SM_PRECISION_FP64 && precision != SM_PRECISION_MIXED) {
+  if (precision != SM_PRECISION_FP64 && precision != SM_PRECISION_MIXED &&
+      precision != SM_PRECISION_MIXED_LEARNED) {
     set_error("sm_ctx_set_precision: unknown precision mode");
     return SM_ERR_VALUE;
   }

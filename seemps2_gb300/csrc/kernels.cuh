@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace sm {
@@ -13,10 +15,31 @@ namespace sm {
 // Context: scratch device buffers (grown on demand, reused across calls) and a
 // small pinned host block for reading back ranks / scalars.
 // ---------------------------------------------------------------------------
+// BF16 copy of the rank predictor (sm_rank_model_set), used for inference.
+struct RankModel {
+  bool loaded = false;
+  int layers = 0;
+  int dims[9] = {};
+  __nv_bfloat16* w = nullptr;
+  float* b = nullptr;
+};
+
 struct Ctx {
   int device = 0;
   int num_sms = 0;
-  int precision = 0;  // SM_PRECISION_FP64 or SM_PRECISION_MIXED
+  int precision = 0;  // SM_PRECISION_FP64, SM_PRECISION_MIXED or SM_PRECISION_MIXED_LEARNED
+  // rank features: position of the split being made (set by the sweep
+  // driver), the previous split's kept rank and leading singular values,
+  // the model, and the recorder (features, kept rank) of every split
+  int split_site = -1, split_n = 0;
+  int prev_rank = 0;
+  std::vector<double> prev_s;
+  const double* last_s = nullptr;  // device: sorted singular values of the last split
+  int last_len = 0;
+  RankModel model;
+  bool record = false;
+  std::vector<float> rec_x;
+  std::vector<int> rec_y;
   void* pinned = nullptr;  // 64 KB of pinned host memory
   std::map<std::string, std::pair<void*, size_t>> bufs;
   std::map<const void*, int> coop_blocks;  // per-kernel co-resident CTA limit
@@ -114,6 +137,12 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
               int left_mode, T* left, int right_mode, T* right, double* s_out,
               SplitResult* res);
 
+// --- mlp.cu ----------------------------------------------------------------
+// The SM_RANK_FEATURES features of a split of size k about to be made.
+void rank_features(const Ctx& ctx, int k, const sm_strategy& st, float* f);
+// Kept rank of that split predicted by the context's model (1..k).
+int rank_predict(Ctx& ctx, cudaStream_t st, int k, const sm_strategy& strat, int* out);
+
 // --- svd_mixed.cu ------------------------------------------------------------
 // Whether the 16-CTA cluster factorisation holds W (kw x l) on this GPU.
 template <typename T>
@@ -122,9 +151,12 @@ bool split_cluster_fits(int kw, int l);
 // cluster.  Writes kcap rows (FP64, ld = l, zero past the iteration's rows)
 // and their norms; ctl receives status / sweeps / nact = rows of R kept;
 // info[0] = |A|_F^2 (FP64), info[1] = trailing weight dropped by the QR.
+// With Z (s_rows x l, FP64) given, the QR is skipped and the Jacobi runs on
+// the rows of Z (a sketch Omega^H W of W's row space); info[0] is still
+// |A|_F^2.
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info);
+                      JacobiCtl* ctl, double* info, const T* Z = nullptr, int s_rows = 0);
 
 }  // namespace sm

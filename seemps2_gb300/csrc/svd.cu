@@ -983,6 +983,8 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     set_error("SVD did not converge");
     return SM_ERR_LINALG;
   }
+  ctx.last_s = s_sorted;
+  ctx.last_len = k;
   if (s_out)
     SM_CUDA_CHECK(cudaMemcpyAsync(s_out, s_sorted, sizeof(double) * k, cudaMemcpyDeviceToDevice, st));
   if (ctx.trace) {
@@ -1077,6 +1079,7 @@ constexpr int kMixedRefine = 2;    // refinement steps
 constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
 constexpr double kMixedCutAmp = 1e-6;  // largest kept/dropped coupling (angle s_i / |A|)
 constexpr double kMixedMinTol = 1e-14;   // smallest relative-norm tolerance taken in mixed
+constexpr int kSketchOversample = 10;    // sketch rows beyond the predicted rank
 
 template <typename T>
 __global__ void k_gather_rows(const T* __restrict__ rows, int l, const int* __restrict__ perm,
@@ -1189,13 +1192,41 @@ __global__ void k_exact_weight_rank(SplitResult* res, const double* __restrict__
 }
 
 // Also info[2] = s[0], info[3] = s[D-1] for the host's checks.
-__global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, double* info) {
+// info[7] = |A|^2 - sum of all cnt values^2: the weight outside the rows'
+// span (what a sketch missed).
+__global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, double* info, int cnt) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double kept = 0.0;
-  for (int j = 0; j < res->D; ++j) kept += s[j] * s[j];
-  res->err2 = fmax(0.0, info[0] - kept);
+  double kept_D = 0.0, kept_all = 0.0;
+  for (int j = 0; j < cnt; ++j) {
+    if (j == res->D) kept_D = kept_all;
+    kept_all += s[j] * s[j];
+  }
+  if (res->D >= cnt) kept_D = kept_all;
+  res->err2 = fmax(0.0, info[0] - kept_D);
   info[2] = s[0];
   info[3] = s[max(res->D, 1) - 1];
+  info[7] = fmax(0.0, info[0] - kept_all);
+}
+
+// Fixed Gaussian sketch Omega (rows x cols, row-major): entry e from a
+// counter-based hash of e (splitmix64) through Box-Muller, so equal shapes
+// always get the same matrix.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+template <typename T>
+__global__ void k_gauss_sketch(T* __restrict__ O, int rows, int cols) {
+  const size_t tot = (size_t)rows * cols;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long h = splitmix64(e * 2 + 1), g = splitmix64(e * 2 + 2);
+    const double u1 = ((h >> 11) + 1.0) * (1.0 / 9007199254740993.0);  // (0, 1]
+    const double u2 = (g >> 11) * (1.0 / 9007199254740992.0);
+    O[e] = S<T>::from_real(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+  }
 }
 
 // Largest state change left by the coupling between a kept row i and a
@@ -1282,7 +1313,7 @@ double allowed_discard(const sm_strategy& st, double norm2, double s0, int k, in
 
 template <typename T>
 int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
-                    bool want_u, T* left, T* right, SplitResult* out, bool* done) {
+                    bool want_u, T* left, T* right, SplitResult* out, bool* done, int sketch) {
   *done = false;
   const int kw = want_u ? n : m;
   const int l = want_u ? m : n;
@@ -1321,8 +1352,27 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   else thr_abs = 1e-2 * strat.tolerance * strat.tolerance;
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+  T* Zs = nullptr;
+  if (sketch > 0) {
+    // randomized range finder: Z = Omega^T W (sketch x l), Omega a fixed
+    // Gaussian kw x sketch matrix; Z's rows span W's leading row space
+    T* Om;
+    SM_CHECK(ctx.scratch("mx.omega", (size_t)kw * sketch, &Om));
+    SM_CHECK(ctx.scratch("mx.sketch", (size_t)sketch * l, &Zs));
+    k_gauss_sketch<T><<<grid_for((size_t)kw * sketch), 256, 0, st>>>(Om, kw, sketch);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    const T one1 = S<T>::one(), zero1 = S<T>::zero();
+    if (want_u)  // W = A^T: Z = Omega^T A^T
+      SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_T, SM_OP_T, sketch, m, n, one1, Om, sketch, A, n, zero1,
+                           Zs, m));
+    else  // W = A: Z = Omega^T A
+      SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_T, SM_OP_N, sketch, n, m, one1, Om, sketch, A, n, zero1,
+                           Zs, n));
+    ctx.stats.mixed_sketched += 1;
+  }
   SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
-                                info));
+                                info, Zs, sketch));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
   struct Head {
     JacobiCtl c;
@@ -1337,7 +1387,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
                                        (int)sort_smem));
   k_sort_truncate<<<1, 1024, sort_smem, st>>>(nrm, kcap, strat, perm, s_sorted, errors, ctl, res);
   note_launch();
-  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info);
+  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info, kcap);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   Head* h = reinterpret_cast<Head*>(ctx.pinned);
@@ -1423,7 +1473,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     k_exact_weight_rank<<<1, 1, 0, st>>>(res, s_sorted, cnt, strat, info);
     note_launch();
   }
-  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info);
+  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info, cnt);
   note_launch();
   SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
   k_cut_check<T><<<1, 256, 0, st>>>(Gb, cnt, perm, s_sorted, res, kMixedBlind, info);
@@ -1432,7 +1482,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SplitResult* hr = reinterpret_cast<SplitResult*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(hr, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
   double* hs = reinterpret_cast<double*>(hr + 1);
-  SM_CUDA_CHECK(cudaMemcpyAsync(hs, info + 2, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaMemcpyAsync(hs, info + 2, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
   const double s0 = hs[0];
   const SplitResult r = *hr;
@@ -1444,12 +1494,16 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   const double s_last = hs[1];
   const double cut_angle = hs[2];
   const bool blind = !exact_rule && s_last < kMixedBlind * s0;
+  // a sketch that missed weight the rank may need: more than 1% of what the
+  // tolerance allows (and more than 1e-12 of |A|^2) outside the rows' span
+  const bool missed = sketch > 0 && hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
   const bool coupled = !(cut_angle <= kMixedCutAmp);
   const bool over = D < strat.max_bond_dimension && D < k &&
                     r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
-  if (blind || coupled || over) {
+  if (blind || coupled || over || missed) {
     ctx.stats.mixed_fallbacks += 1;
     if (coupled) ctx.stats.mixed_fallback_cut += 1;
+    else if (missed) ctx.stats.mixed_fallback_sketch += 1;
     else ctx.stats.mixed_fallback_fp32 += 1;
     return SM_OK;
   }
@@ -1463,6 +1517,8 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   *out = r;
   out->status = 0;
   ctx.stats.splits += 1;
+  ctx.last_s = s_sorted;
+  ctx.last_len = cnt;
   if (ctx.trace) {
     const size_t off = ctx.tr_s.size();
     ctx.tr_s.resize(off + cnt);
@@ -1478,18 +1534,27 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
 }
 
 template <typename T>
-int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
-              int left_mode, T* left, int right_mode, T* right, double* s_out,
-              SplitResult* out) {
+static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
+                         const sm_strategy& strat, int left_mode, T* left, int right_mode, T* right,
+                         double* s_out, SplitResult* out) {
   if (m <= 0 || n <= 0) {
     set_error("svd: empty matrix");
     return SM_ERR_VALUE;
   }
   const bool xu = left_mode == OUT_U && right_mode == OUT_SVT;
   const bool xv = left_mode == OUT_US && right_mode == OUT_VT;
-  if ((xu || xv) && ctx.precision == SM_PRECISION_MIXED && !s_out) {
+  if ((xu || xv) && ctx.precision != SM_PRECISION_FP64 && !s_out) {
+    int sketch = 0;
+    if (ctx.precision == SM_PRECISION_MIXED_LEARNED && ctx.model.loaded &&
+        std::min(m, n) >= kMixedMinRank && strat.method == SM_RELATIVE_NORM_SQUARED_ERROR &&
+        strat.tolerance >= kMixedMinTol) {
+      int r = 0;
+      SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
+      sketch = std::min(std::min(m, n), r + kSketchOversample);
+      ctx.stats.rank_predicted_sum += r;
+    }
     bool done = false;
-    SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done));
+    SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, sketch));
     if (done) return SM_OK;
   }
   if (xu) return svd_split_xfree<T>(ctx, st, A, m, n, strat, true, left, right, s_out, out);
@@ -1592,6 +1657,8 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     set_error("SVD did not converge");
     return SM_ERR_LINALG;
   }
+  ctx.last_s = s_sorted;
+  ctx.last_len = k;
   if (s_out)
     SM_CUDA_CHECK(cudaMemcpyAsync(s_out, s_sorted, sizeof(double) * k, cudaMemcpyDeviceToDevice, st));
   if (ctx.trace) {
@@ -1612,6 +1679,37 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
                                                    s_sorted, left_mode, left, right_mode, right);
                                                    note_launch();
     SM_CUDA_CHECK(cudaGetLastError());
+  }
+  return SM_OK;
+}
+
+// Every split: features of the split (when recording or predicting), the
+// split itself, then the record (features, kept rank) and the previous-split
+// state the next split's features use.
+template <typename T>
+int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
+              int left_mode, T* left, int right_mode, T* right, double* s_out,
+              SplitResult* out) {
+  const bool feat = ctx.record || ctx.precision == SM_PRECISION_MIXED_LEARNED;
+  float f[SM_RANK_FEATURES];
+  if (feat) rank_features(ctx, std::min(m, n), strat, f);
+  ctx.last_s = nullptr;
+  ctx.last_len = 0;
+  SM_CHECK(svd_split_run<T>(ctx, st, A, m, n, strat, left_mode, left, right_mode, right, s_out,
+                            out));
+  if (feat) {
+    if (ctx.record) {
+      ctx.rec_x.insert(ctx.rec_x.end(), f, f + SM_RANK_FEATURES);
+      ctx.rec_y.push_back(out->D);
+    }
+    ctx.prev_rank = out->D;
+    const int c = std::min(32, ctx.last_len);
+    ctx.prev_s.assign(c, 0.0);
+    if (c > 0 && ctx.last_s) {
+      SM_CUDA_CHECK(cudaMemcpyAsync(ctx.prev_s.data(), ctx.last_s, sizeof(double) * c,
+                                    cudaMemcpyDeviceToHost, st));
+      SM_CUDA_CHECK(cudaStreamSynchronize(st));
+    }
   }
   return SM_OK;
 }

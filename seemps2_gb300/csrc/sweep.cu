@@ -56,7 +56,13 @@ struct Sweeper {
   double* dsc = nullptr;  // device scalars
   int splits = 0;
 
-  Sweeper(Ctx& c, cudaStream_t stream, const sm_strategy& strat) : ctx(c), st(stream), s(strat) {}
+  // each call starts the split features afresh (no previous split)
+  Sweeper(Ctx& c, cudaStream_t stream, const sm_strategy& strat) : ctx(c), st(stream), s(strat) {
+    ctx.prev_s.clear();
+    ctx.prev_rank = 0;
+    ctx.split_site = -1;
+    ctx.split_n = 0;
+  }
 
   size_t site_elems(int i) const { return (size_t)bb[i] * d[i] * bb[i + 1]; }
 
@@ -74,6 +80,8 @@ struct Sweeper {
   int canon_right(int i, double* err) {
     const int a = bb[i], di = d[i], b = bb[i + 1];
     SplitResult r;
+    ctx.split_site = i;
+    ctx.split_n = L;
     SM_CHECK(svd_split<T>(ctx, st, bra[i], a * di, b, s, OUT_U, bra[i], OUT_SVT, tmp, nullptr, &r));
     ++splits;
     const int D = r.D;
@@ -92,6 +100,8 @@ struct Sweeper {
   int canon_left(int i, double* err) {
     const int a = bb[i], di = d[i], b = bb[i + 1];
     SplitResult r;
+    ctx.split_site = i;
+    ctx.split_n = L;
     SM_CHECK(svd_split<T>(ctx, st, bra[i], a, di * b, s, OUT_US, tmp, OUT_VT, bra[i], nullptr, &r));
     ++splits;
     const int D = r.D;
@@ -226,6 +236,8 @@ struct Sweeper {
   int step_right(int n) {
     SM_CHECK(two_site(n));
     SplitResult r;
+    ctx.split_site = n;
+    ctx.split_n = L;
     SM_CHECK(svd_split<T>(ctx, st, AA, bb[n] * d[n], d[n + 1] * bb[n + 2], s, OUT_U, bra[n], OUT_SVT,
                           bra[n + 1], nullptr, &r));
     ++splits;
@@ -237,6 +249,8 @@ struct Sweeper {
   int step_left(int n) {
     SM_CHECK(two_site(n));
     SplitResult r;
+    ctx.split_site = n;
+    ctx.split_n = L;
     SM_CHECK(svd_split<T>(ctx, st, AA, bb[n] * d[n], d[n + 1] * bb[n + 2], s, OUT_US, bra[n], OUT_VT,
                           bra[n + 1], nullptr, &r));
     ++splits;

@@ -1,0 +1,147 @@
+"""The learned rank predictor: GPU kernels against the CPU oracle, recording,
+and what the trained network gains over the method without it.
+
+Bars: forward within 1e-5 (relative, FP32 vs the FP64 oracle), gradients
+within 1e-4 of the largest gradient entry, one Adam step within 1e-6, BF16
+inference within 0.05 (relative) of the FP32 network; the trained network's
+mean |error| in log2 rank below the no-network baseline's (the previous
+split's rank); mixed+learned MPO.apply within 1e-10 fidelity of the FP64
+oracle with the sketch in use.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+from oracle import seemps_oracle as so
+from tests.gpu_util import mps_np
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import seemps2_gb300 as sg  # noqa: E402
+from seemps2_gb300 import _lib, learned  # noqa: E402
+
+DIMS = (37, 64, 48, 1)
+
+
+def _model(seed=3, dims=DIMS):
+    p = mo.init_params(dims, np.random.default_rng(seed))
+    return learned.RankModel(dims, params=p), p
+
+
+def test_forward_matches_oracle():
+    m, p = _model()
+    X = np.random.default_rng(4).normal(size=(33, DIMS[0])).astype(np.float32)
+    y_gpu, _ = m.forward(torch.from_numpy(X).cuda())
+    y_ref, _ = mo.forward(p.astype(np.float32).astype(np.float64), DIMS, X.astype(np.float64))
+    y_gpu = y_gpu.cpu().numpy()
+    assert np.max(np.abs(y_gpu - y_ref.reshape(-1))) <= 1e-5 * max(1.0, np.abs(y_ref).max())
+
+
+@pytest.mark.parametrize("batch", [1, 17, 256])
+def test_gradients_match_oracle(batch):
+    m, p = _model()
+    rng = np.random.default_rng(5)
+    X = rng.normal(size=(batch, DIMS[0])).astype(np.float32)
+    y = rng.normal(size=batch).astype(np.float32)
+    loss, g = m.loss_and_grad(torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda())
+    p64 = p.astype(np.float32).astype(np.float64)
+    yhat, cache = mo.forward(p64, DIMS, X.astype(np.float64))
+    l_ref, dy = mo.mse(yhat, y.astype(np.float64))
+    g_ref = mo.backward(p64, DIMS, X.astype(np.float64), cache, dy)
+    assert abs(float(loss.item()) - l_ref) <= 1e-5 * max(1.0, l_ref)
+    g = g.cpu().numpy()
+    assert np.max(np.abs(g - g_ref)) <= 1e-4 * np.abs(g_ref).max()
+
+
+def test_adam_step_matches_oracle():
+    rng = np.random.default_rng(6)
+    n = 1000
+    p = rng.normal(size=n).astype(np.float32)
+    g = rng.normal(size=n).astype(np.float32)
+    m = (0.1 * rng.normal(size=n)).astype(np.float32)
+    v = np.abs(rng.normal(size=n)).astype(np.float32)
+    dev = [torch.from_numpy(x.copy()).cuda() for x in (p, g, m, v)]
+    _lib.check(_lib.load().sm_adam_step(_lib.context(), dev[0].data_ptr(), dev[1].data_ptr(),
+                                        dev[2].data_ptr(), dev[3].data_ptr(), n, 1e-3, 0.9, 0.999,
+                                        1e-8, 7, _lib.stream_handle()))
+    pr, mr, vr = (x.astype(np.float64) for x in (p, m, v))
+    mo.adam_step(pr, g.astype(np.float64), mr, vr, 1e-3, 0.9, 0.999, 1e-8, 7)
+    assert np.max(np.abs(dev[0].cpu().numpy() - pr)) <= 1e-6
+    assert np.max(np.abs(dev[2].cpu().numpy() - mr)) <= 1e-6
+
+
+def test_bf16_inference_matches_fp32_network():
+    dims = learned.DIMS
+    m, p = _model(seed=8, dims=dims)
+    rng = np.random.default_rng(9)
+    X = rng.normal(size=(64, dims[0])).astype(np.float32) * 3.0 + 1.0
+    m.mean = X.mean(axis=0)
+    m.std = X.std(axis=0) + 1e-3
+    m.install()
+    y = m.predict_log2(X)
+    y_ref, _ = mo.forward(p.astype(np.float32).astype(np.float64), dims,
+                          ((X - m.mean) / m.std).astype(np.float64))
+    assert np.max(np.abs(y - y_ref.reshape(-1))) <= 0.05 * max(1.0, np.abs(y_ref).max())
+
+
+def test_records_every_split_with_its_rank():
+    rng = np.random.default_rng(2)
+    mps = so.random_mps(2, 10, 16, rng)
+    mpo = so.random_mpo(2, 10, 3, rng)
+    st = sg.DEFAULT_STRATEGY.replace(tolerance=1e-8, max_bond_dimension=24, max_sweeps=2,
+                                     simplification_tolerance=0.0)
+    with _lib.SplitTrace() as tr, learned.record_truncations() as rec:
+        sg.MPO(mpo, st).apply(sg.MPS(mps), strategy=st)
+    assert rec.X.shape == (len(tr.ranks), 37)
+    assert rec.D.tolist() == tr.ranks
+    # the previous-rank feature is log2(1 + the previous split's rank) within a
+    # sweep call (each call starts from 0)
+    chained = rec.X[1:, 34] > 0
+    assert chained.sum() >= len(tr.ranks) // 2
+    assert np.allclose(rec.X[1:, 34][chained], np.log2(1.0 + rec.D[:-1][chained]))
+
+
+@pytest.fixture(scope="module")
+def trained():
+    X, D = learned.record_dataset(count=45, seed=11)
+    model = learned.RankModel.initial(seed=1)
+    hist = model.fit(X, D, epochs=30)
+    Xt, Dt = learned.record_dataset(count=15, seed=12)
+    return model, hist, Xt, Dt
+
+
+def test_trained_network_beats_the_baseline(trained):
+    model, hist, Xt, Dt = trained
+    assert hist[-1] < 0.25 * hist[0]
+    model.install()
+    y = np.log2(np.maximum(Dt, 1))
+    err_net = np.mean(np.abs(model.predict_log2(Xt) - y))
+    err_base = np.mean(np.abs(learned.baseline_log2(Xt) - y))
+    assert err_net < err_base, (err_net, err_base)
+
+
+def test_mixed_learned_apply_matches_oracle(trained):
+    model, *_ = trained
+    model.install()
+    rng = np.random.default_rng(7)
+    n, chi = 14, 64
+    mps, mpo = learned.laplacian_case(n, chi, rng)
+    kw = dict(tolerance=1e-12, max_bond_dimension=chi, max_sweeps=2, simplification_tolerance=0.0)
+    st = sg.DEFAULT_STRATEGY.replace(**kw)
+    sg.set_precision("mixed+learned")
+    _lib.stats_reset()
+    try:
+        out = sg.MPO(mpo, st).apply(sg.MPS(mps), strategy=st)
+        stats = _lib.stats_read()
+    finally:
+        sg.set_precision("fp64")
+    res = so.mpo_apply(mpo, mps, so.DEFAULT_STRATEGY.replace(**kw))
+    assert stats["mixed_sketched"] > 5
+    assert stats["mixed_fallbacks"] <= 0.3 * stats["mixed_splits"]
+    fe = so.fidelity_error(mps_np(out), res.tensors)
+    assert fe < 1e-10, fe
