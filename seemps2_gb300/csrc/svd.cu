@@ -1080,6 +1080,7 @@ constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage 
 constexpr double kMixedCutAmp = 1e-6;  // largest kept/dropped coupling (angle s_i / |A|)
 constexpr double kMixedMinTol = 1e-14;   // smallest relative-norm tolerance taken in mixed
 constexpr int kSketchOversample = 10;    // sketch rows beyond the predicted rank
+constexpr double kSketchMargin = 1.15;   // relative margin on the predicted rank
 
 template <typename T>
 __global__ void k_gather_rows(const T* __restrict__ rows, int l, const int* __restrict__ perm,
@@ -1313,8 +1314,10 @@ double allowed_discard(const sm_strategy& st, double norm2, double s0, int k, in
 
 template <typename T>
 int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
-                    bool want_u, T* left, T* right, SplitResult* out, bool* done, int sketch) {
+                    bool want_u, T* left, T* right, SplitResult* out, bool* done, int sketch,
+                    bool* missed_out) {
   *done = false;
+  *missed_out = false;
   const int kw = want_u ? n : m;
   const int l = want_u ? m : n;
   const int k = std::min(kw, l);
@@ -1500,10 +1503,15 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   const bool coupled = !(cut_angle <= kMixedCutAmp);
   const bool over = D < strat.max_bond_dimension && D < k &&
                     r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
-  if (blind || coupled || over || missed) {
+  if (missed && !blind && !coupled) {
+    // the sketch was too small: the caller retries with the rank-revealing QR
+    ctx.stats.mixed_fallback_sketch += 1;
+    *missed_out = true;
+    return SM_OK;
+  }
+  if (blind || coupled || over) {
     ctx.stats.mixed_fallbacks += 1;
     if (coupled) ctx.stats.mixed_fallback_cut += 1;
-    else if (missed) ctx.stats.mixed_fallback_sketch += 1;
     else ctx.stats.mixed_fallback_fp32 += 1;
     return SM_OK;
   }
@@ -1550,11 +1558,16 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
         strat.tolerance >= kMixedMinTol) {
       int r = 0;
       SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
-      sketch = std::min(std::min(m, n), r + kSketchOversample);
+      sketch = std::min(std::min(m, n), (int)std::ceil(kSketchMargin * r) + kSketchOversample);
       ctx.stats.rank_predicted_sum += r;
     }
-    bool done = false;
-    SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, sketch));
+    bool done = false, missed = false;
+    SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, sketch,
+                                &missed));
+    if (done) return SM_OK;
+    if (missed)  // predicted rank too small: the rank-revealing QR instead of the sketch
+      SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, 0,
+                                  &missed));
     if (done) return SM_OK;
   }
   if (xu) return svd_split_xfree<T>(ctx, st, A, m, n, strat, true, left, right, s_out, out);

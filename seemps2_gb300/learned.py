@@ -8,9 +8,9 @@ the library's own kernels (``sm_mlp_forward`` / ``sm_mlp_backward`` /
 ``sm_mse_loss`` / ``sm_adam_step``) on truncations that the FP64 method records
 (``sm_rank_features_record``).  Installed with :meth:`RankModel.install` and
 ``set_precision("mixed+learned")``, each mixed split replaces its FP32
-rank-revealing QR by a fixed Gaussian sketch of (predicted rank + 10) rows; the
-exact discarded weight still decides, and sends a split whose sketch missed
-weight to the FP64 Jacobi SVD.
+rank-revealing QR by a fixed Gaussian sketch of (1.15 predicted rank + 10)
+rows; a split whose sketch missed weight is redone with the QR, and the exact
+discarded weight still sends tolerance violations to the FP64 Jacobi SVD.
 
 Input standardisation is folded into the first layer when the model is
 installed, so the device sees raw features.

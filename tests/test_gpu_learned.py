@@ -141,7 +141,11 @@ def test_mixed_learned_apply_matches_oracle(trained):
     finally:
         sg.set_precision("fp64")
     res = so.mpo_apply(mpo, mps, so.DEFAULT_STRATEGY.replace(**kw))
-    assert stats["mixed_sketched"] > 5
-    assert stats["mixed_fallbacks"] <= 0.3 * stats["mixed_splits"]
+    info = {k: stats[k] for k in ("mixed_splits", "mixed_sketched", "mixed_fallbacks",
+                                  "mixed_fallback_sketch", "mixed_fallback_fp32",
+                                  "mixed_fallback_cut", "rank_predicted_sum")}
+    assert stats["mixed_sketched"] > 5, info
+    # sketches that missed weight are redone with the QR, not counted as FP64 fallbacks
+    assert stats["mixed_fallbacks"] <= 0.3 * stats["mixed_sketched"], info
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-10, fe
