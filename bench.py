@@ -259,7 +259,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=30)
     ap.add_argument("--chi", type=int, default=256)
-    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--form", default="mixed+learned", choices=["plain", "mixed", "mixed+learned"],
+                    help="plain = FP64 splits (reference ranks); mixed = FP32 cluster "
+                         "factorisation + FP64 refinement; mixed+learned = mixed with the rank "
+                         "predictor sizing a randomized sketch (the metric's headline form)")
+    ap.add_argument("--rank-model", default=None,
+                    help="trained rank predictor (.npz); trained here when absent")
+    ap.add_argument("--train-count", type=int, default=90,
+                    help="training workloads recorded when the predictor is trained here")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--split-case", type=int, nargs=2, metavar=("M", "N"),
                     help="time single M x N two-site splits in both precision modes and exit")
@@ -289,13 +296,48 @@ def main():
 
     mps_h, mpo_h = make_workload(args.n, args.chi)
     st = sg.DEFAULT_STRATEGY.replace(**strategy_kwargs(args.chi))
-    sg.set_precision("fp64" if args.form == "plain" else "mixed")
     psi = sg.MPS(mps_h)
     O = sg.MPO(mpo_h, st)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     def step():
         return O.apply(psi, strategy=st)
+
+    # ---- rank predictor (outside every timed region) ---------------------------
+    learned_info = None
+    if args.form == "mixed+learned":
+        from seemps2_gb300 import learned
+
+        t0 = time.perf_counter()
+        if args.rank_model and os.path.exists(args.rank_model):
+            model = learned.RankModel.load(args.rank_model)
+            learned_info = {"model": args.rank_model}
+        else:
+            model, rep = learned.train_default(count=args.train_count, epochs=40, seed=1)
+            learned_info = {"model": "trained in this run on the GPU (library kernels)", **rep}
+        model.install()
+        learned_info["setup_s"] = time.perf_counter() - t0
+
+    # ---- plain FP64 form on the same workload (the metric's comparison) -------
+    plain = None
+    if args.form != "plain":
+        sg.set_precision("fp64")
+        step()
+        torch.cuda.synchronize()
+        pt = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step()
+            e1.record()
+            e1.synchronize()
+            pt.append(e0.elapsed_time(e1))
+        psw = sg.state.last_report["sweeps"]
+        plain = {"value": psw * len(pt) / (sum(pt) / 1e3), "unit": "sweeps/s",
+                 "ms_per_step": sum(pt) / len(pt)}
+    sg.set_precision({"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed+learned"}[args.form])
 
     for _ in range(max(3, args.warmup)):
         out = step()
@@ -360,20 +402,25 @@ def main():
     stt = _lib.stats_read()
     _lib.stats_reset(timing=False)
     peak = fp64_peak(torch, _lib)
-    achieved = stt["jacobi_flops"] / (stt["jacobi_ms"] / 1e3) if stt["jacobi_ms"] else 0.0
-    gemm_rate = stt["gemm_flops"] / (stt["gemm_ms"] / 1e3) if stt["gemm_ms"] else 0.0
+    # the dominant FP64 kernel of the step (event-timed per launch in this step)
+    cands = {"k_jacobi (one-sided Jacobi SVD, FP64)": ("jacobi", stt["jacobi_flops"],
+                                                      stt["jacobi_ms"], stt["jacobi_launches"]),
+             "k_gemm (SIMT FP64 GEMM, split-K)": ("gemm", stt["gemm_flops"], stt["gemm_ms"],
+                                                  stt["gemm_launches"])}
+    kname, (tag, kfl, kms, kl) = max(cands.items(), key=lambda kv: kv[1][2])
+    achieved = kfl / (kms / 1e3) if kms else 0.0
     roofline = {
-        "bound": "fp64", "kernel": "k_jacobi (one-sided Jacobi SVD, FP64)",
+        "bound": "fp64", "kernel": kname,
         "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
         "frac": achieved / peak if peak else None, "traffic": None,
         "peak_source": "measured in this run: the library's FP64 GEMM at 2048^3 (GB300 FP64 has "
                        "no tensor-core path; MEASURED_PEAKS.json lists HBM and bf16 only)",
-        "flops_per_launch": stt["jacobi_flops"] / max(1, stt["jacobi_launches"]),
-        "launches_per_step": stt["jacobi_launches"],
-        "avg_launch_ms": stt["jacobi_ms"] / max(1, stt["jacobi_launches"]),
-        "share_of_step": stt["jacobi_ms"] / inst_ms if inst_ms else None,
-        "avg_jacobi_sweeps": stt["jacobi_sweeps"] / max(1, stt["jacobi_launches"]),
-        "gemm_tflops": gemm_rate / 1e12, "gemm_share_of_step": stt["gemm_ms"] / inst_ms if inst_ms else None,
+        "flops_per_launch": kfl / max(1, kl), "launches_per_step": kl,
+        "avg_launch_ms": kms / max(1, kl), "share_of_step": kms / inst_ms if inst_ms else None,
+        "jacobi_share_of_step": stt["jacobi_ms"] / inst_ms if inst_ms else None,
+        "gemm_share_of_step": stt["gemm_ms"] / inst_ms if inst_ms else None,
+        "cluster_share_of_step": stt["cluster_ms"] / inst_ms if inst_ms else None,
+        "cluster_bound": "latency (FP32 rotations on 16 SMs, one cluster barrier per block round)",
     }
 
     # ---- CPU baseline (oracle, bounded sample) -------------------------------
@@ -412,7 +459,10 @@ def main():
             "gpu_launches": launches, "bonds_out": out.bond_dimensions()[: args.n // 2 + 1],
             "error": out.error(), "oracle_check": oracle_check,
         }
-        if args.form == "mixed":
+        if plain:
+            line["plain_fp64"] = plain
+            line["speedup_vs_plain_fp64"] = value / plain["value"] if plain["value"] else None
+        if args.form != "plain":
             k = max(1, args.steps)
             line["mixed"] = {
                 "splits_per_step": timed_stats["mixed_splits"] / k,
@@ -423,7 +473,13 @@ def main():
                 "cluster_jacobi_ms_per_step": timed_stats["cluster_jacobi_ms"] / k,
                 "fallbacks_coupling_per_step": timed_stats["mixed_fallback_cut"] / k,
                 "fallbacks_fp32_per_step": timed_stats["mixed_fallback_fp32"] / k,
+                "sketched_per_step": timed_stats["mixed_sketched"] / k,
+                "sketch_misses_per_step": timed_stats["mixed_fallback_sketch"] / k,
+                "mean_predicted_rank": timed_stats["rank_predicted_sum"]
+                / max(1, timed_stats["mixed_sketched"]),
             }
+            if learned_info:
+                line["learned"] = learned_info
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

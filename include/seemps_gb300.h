@@ -101,12 +101,12 @@ int sm_ctx_destroy(void* ctx);
  *                      from the reference's at the tolerance boundary. */
 enum { SM_PRECISION_FP64 = 0, SM_PRECISION_MIXED = 1, SM_PRECISION_MIXED_LEARNED = 2 };
 /* SM_PRECISION_MIXED_LEARNED: as SM_PRECISION_MIXED, but the rank predictor set
- * with sm_rank_model_set predicts each split's kept rank r and a randomized
- * range finder (an FP64 GEMM with a fixed Gaussian sketch of 1.15 r + 10 rows)
- * replaces the FP32 rank-revealing QR; a split whose sketch missed weight
- * (more than 1% of what the tolerance allows outside the sketch's span) is
- * redone with the QR, and the exact discarded-weight check still sends
- * tolerance violations to the FP64 Jacobi SVD. */
+ * with sm_rank_model_set predicts each split's kept rank r and the FP32
+ * rank-revealing QR stops after ceil(1.15 r) + 10 steps at most; a split whose
+ * capped QR left weight behind (more than 1% of what the tolerance allows
+ * outside the rows' span, computed exactly after the refinement) is redone
+ * without the cap, and the exact discarded-weight check still sends tolerance
+ * violations to the FP64 Jacobi SVD. */
 int sm_ctx_set_precision(void* ctx, int precision);
 
 /* ---- rank predictor (no reference counterpart) ------------------------------
@@ -274,8 +274,8 @@ typedef struct sm_stats {
   double cluster_jacobi_ms;/* of which: FP32 Jacobi + store (device timer) */
   int64_t mixed_fallback_cut;  /* fallbacks: kept/dropped coupling left after refinement */
   int64_t mixed_fallback_fp32; /* fallbacks: FP32 stage (convergence, resolution, weight) */
-  int64_t mixed_sketched;      /* mixed splits that used the predicted-rank sketch */
-  int64_t mixed_fallback_sketch; /* sketch missed weight: redone with the FP32 QR */
+  int64_t mixed_sketched;      /* mixed splits whose QR the predicted rank capped */
+  int64_t mixed_fallback_sketch; /* capped QR left weight: redone without the cap */
   int64_t rank_predicted_sum;  /* predicted kept ranks, summed */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);

@@ -151,12 +151,12 @@ bool split_cluster_fits(int kw, int l);
 // cluster.  Writes kcap rows (FP64, ld = l, zero past the iteration's rows)
 // and their norms; ctl receives status / sweeps / nact = rows of R kept;
 // info[0] = |A|_F^2 (FP64), info[1] = trailing weight dropped by the QR.
-// With Z (s_rows x l, FP64) given, the QR is skipped and the Jacobi runs on
-// the rows of Z (a sketch Omega^H W of W's row space); info[0] is still
-// |A|_F^2.
+// qr_cap > 0 stops the QR after that many steps (a predicted rank) even if
+// the trailing weight is still above the threshold; info[1] then holds the
+// weight it left behind.
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, const T* Z = nullptr, int s_rows = 0);
+                      JacobiCtl* ctl, double* info, int qr_cap = 0);
 
 }  // namespace sm

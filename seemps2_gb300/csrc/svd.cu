@@ -1079,8 +1079,8 @@ constexpr int kMixedRefine = 2;    // refinement steps
 constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
 constexpr double kMixedCutAmp = 1e-6;  // largest kept/dropped coupling (angle s_i / |A|)
 constexpr double kMixedMinTol = 1e-14;   // smallest relative-norm tolerance taken in mixed
-constexpr int kSketchOversample = 10;    // sketch rows beyond the predicted rank
-constexpr double kSketchMargin = 1.15;   // relative margin on the predicted rank
+constexpr int kCapOversample = 10;    // QR rows beyond the predicted rank
+constexpr double kCapMargin = 1.15;   // relative margin on the predicted rank
 
 template <typename T>
 __global__ void k_gather_rows(const T* __restrict__ rows, int l, const int* __restrict__ perm,
@@ -1194,7 +1194,7 @@ __global__ void k_exact_weight_rank(SplitResult* res, const double* __restrict__
 
 // Also info[2] = s[0], info[3] = s[D-1] for the host's checks.
 // info[7] = |A|^2 - sum of all cnt values^2: the weight outside the rows'
-// span (what a sketch missed).
+// span (what a capped QR left behind).
 __global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, double* info, int cnt) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double kept_D = 0.0, kept_all = 0.0;
@@ -1207,27 +1207,6 @@ __global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, doub
   info[2] = s[0];
   info[3] = s[max(res->D, 1) - 1];
   info[7] = fmax(0.0, info[0] - kept_all);
-}
-
-// Fixed Gaussian sketch Omega (rows x cols, row-major): entry e from a
-// counter-based hash of e (splitmix64) through Box-Muller, so equal shapes
-// always get the same matrix.
-__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
-  x += 0x9E3779B97F4A7C15ull;
-  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-  return x ^ (x >> 31);
-}
-template <typename T>
-__global__ void k_gauss_sketch(T* __restrict__ O, int rows, int cols) {
-  const size_t tot = (size_t)rows * cols;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const unsigned long long h = splitmix64(e * 2 + 1), g = splitmix64(e * 2 + 2);
-    const double u1 = ((h >> 11) + 1.0) * (1.0 / 9007199254740993.0);  // (0, 1]
-    const double u2 = (g >> 11) * (1.0 / 9007199254740992.0);
-    O[e] = S<T>::from_real(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
-  }
 }
 
 // Largest state change left by the coupling between a kept row i and a
@@ -1314,7 +1293,7 @@ double allowed_discard(const sm_strategy& st, double norm2, double s0, int k, in
 
 template <typename T>
 int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
-                    bool want_u, T* left, T* right, SplitResult* out, bool* done, int sketch,
+                    bool want_u, T* left, T* right, SplitResult* out, bool* done, int qr_cap,
                     bool* missed_out) {
   *done = false;
   *missed_out = false;
@@ -1355,27 +1334,10 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   else thr_abs = 1e-2 * strat.tolerance * strat.tolerance;
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
-  T* Zs = nullptr;
-  if (sketch > 0) {
-    // randomized range finder: Z = Omega^T W (sketch x l), Omega a fixed
-    // Gaussian kw x sketch matrix; Z's rows span W's leading row space
-    T* Om;
-    SM_CHECK(ctx.scratch("mx.omega", (size_t)kw * sketch, &Om));
-    SM_CHECK(ctx.scratch("mx.sketch", (size_t)sketch * l, &Zs));
-    k_gauss_sketch<T><<<grid_for((size_t)kw * sketch), 256, 0, st>>>(Om, kw, sketch);
-    note_launch();
-    SM_CUDA_CHECK(cudaGetLastError());
-    const T one1 = S<T>::one(), zero1 = S<T>::zero();
-    if (want_u)  // W = A^T: Z = Omega^T A^T
-      SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_T, SM_OP_T, sketch, m, n, one1, Om, sketch, A, n, zero1,
-                           Zs, m));
-    else  // W = A: Z = Omega^T A
-      SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_T, SM_OP_N, sketch, n, m, one1, Om, sketch, A, n, zero1,
-                           Zs, n));
-    ctx.stats.mixed_sketched += 1;
-  }
+  // a predicted rank caps the rank-revealing QR (qr_cap rows of R)
+  if (qr_cap > 0) ctx.stats.mixed_sketched += 1;
   SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
-                                info, Zs, sketch));
+                                info, qr_cap));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
   struct Head {
     JacobiCtl c;
@@ -1497,14 +1459,15 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   const double s_last = hs[1];
   const double cut_angle = hs[2];
   const bool blind = !exact_rule && s_last < kMixedBlind * s0;
-  // a sketch that missed weight the rank may need: more than 1% of what the
-  // tolerance allows (and more than 1e-12 of |A|^2) outside the rows' span
-  const bool missed = sketch > 0 && hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
+  // a capped QR that left weight the rank may need: more than 1% of what the
+  // tolerance allows (and more than 1e-12 of |A|^2) outside the rows' span,
+  // computed exactly after the refinement
+  const bool missed = qr_cap > 0 && hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
   const bool coupled = !(cut_angle <= kMixedCutAmp);
   const bool over = D < strat.max_bond_dimension && D < k &&
                     r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
   if (missed && !blind && !coupled) {
-    // the sketch was too small: the caller retries with the rank-revealing QR
+    // the cap was too small: the caller retries with the uncapped QR
     ctx.stats.mixed_fallback_sketch += 1;
     *missed_out = true;
     return SM_OK;
@@ -1552,20 +1515,20 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
   const bool xu = left_mode == OUT_U && right_mode == OUT_SVT;
   const bool xv = left_mode == OUT_US && right_mode == OUT_VT;
   if ((xu || xv) && ctx.precision != SM_PRECISION_FP64 && !s_out) {
-    int sketch = 0;
+    int cap = 0;
     if (ctx.precision == SM_PRECISION_MIXED_LEARNED && ctx.model.loaded &&
         std::min(m, n) >= kMixedMinRank && strat.method == SM_RELATIVE_NORM_SQUARED_ERROR &&
         strat.tolerance >= kMixedMinTol) {
       int r = 0;
       SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
-      sketch = std::min(std::min(m, n), (int)std::ceil(kSketchMargin * r) + kSketchOversample);
+      cap = std::min(std::min(m, n), (int)std::ceil(kCapMargin * r) + kCapOversample);
       ctx.stats.rank_predicted_sum += r;
     }
     bool done = false, missed = false;
-    SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, sketch,
+    SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, cap,
                                 &missed));
     if (done) return SM_OK;
-    if (missed)  // predicted rank too small: the rank-revealing QR instead of the sketch
+    if (missed)  // predicted rank too small: the QR without the cap
       SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, 0,
                                   &missed));
     if (done) return SM_OK;

@@ -124,7 +124,6 @@ struct CtrlS {
   float tau[2];       // reflector tau, by step parity (pushed by the owner)
   float part[2][kCW]; // trailing-weight partials of all CTAs, by step parity
   double part64[kCW]; // |W|^2 partials of all CTAs
-  double partz[kCW];  // |Z|^2 partials of all CTAs (sketch mode)
   float red[kCNW];    // CTA-local reduction scratch
   double red64[kCNW];
 };
@@ -153,7 +152,7 @@ __global__ void __launch_bounds__(kCNT, 1)
     k_split_cluster(const T* __restrict__ A, int n_a, int trans, int kw, int l, double thr_rel,
                     double thr_abs, float tol2, int max_sweeps, T* __restrict__ out_rows,
                     double* __restrict__ out_nrm, int kcap, JacobiCtl* ctl_out,
-                    double* __restrict__ info, const T* __restrict__ Z, int s_rows) {
+                    double* __restrict__ info, int qr_cap) {
   using F = typename F32<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
@@ -162,7 +161,8 @@ __global__ void __launch_bounds__(kCNT, 1)
   const int gw = rank * kCNW + warp;
   const int ncs = (l + kCW - 1) / kCW;  // column slots per CTA
   const int kmax = min(kw, l);
-  const bool sketch = Z != nullptr;
+  // a learned rank caps the QR steps (0: the trailing weight alone decides)
+  const int qsteps = qr_cap > 0 ? min(kmax, qr_cap) : kmax;
   constexpr int LP = 32 * E;
 
   F* cols = reinterpret_cast<F*>(smem_raw);        // [ncs][kw], phase 1
@@ -195,39 +195,18 @@ __global__ void __launch_bounds__(kCNT, 1)
       for (int w = 0; w < kCNW; ++w) t += ctrl->red64[w];
       cluster.map_shared_rank(ctrl, tid)->part64[rank] = t;
     }
-    if (sketch) {
-      __syncthreads();
-      double az = 0.0;
-      const size_t tot = (size_t)s_rows * l;
-      for (size_t e = (size_t)rank * kCNT + tid; e < tot; e += (size_t)kCW * kCNT)
-        az += S<T>::abs2(Z[e]);
-      az = warp_sum(az);
-      if (lane == 0) ctrl->red64[warp] = az;
-      __syncthreads();
-      if (tid < kCW) {
-        double t = 0.0;
-        for (int w = 0; w < kCNW; ++w) t += ctrl->red64[w];
-        cluster.map_shared_rank(ctrl, tid)->partz[rank] = t;
-      }
-    }
   }
   cluster.sync();
-  double norm2 = 0.0, normz2 = 0.0;
+  double norm2 = 0.0;
   for (int r = 0; r < kCW; ++r) norm2 += ctrl->part64[r];
-  if (sketch)
-    for (int r = 0; r < kCW; ++r) normz2 += ctrl->partz[r];
-  // rows are held as (rows of W or Z) / |W or Z|_F in FP32
-  const double nrm = sqrt(sketch ? normz2 : norm2);
+  const double nrm = sqrt(norm2);
   const double scale = nrm > 0.0 ? 1.0 / nrm : 1.0;
   // stop once the trailing block holds at most max(thr_rel |W|^2, thr_abs)
   const float thr = (float)fmax(thr_rel, norm2 > 0.0 ? thr_abs / norm2 : 0.0);
-  if (!sketch) {
-    for (int s = warp; s < ncs; s += kCNW) {
-      const int c = rank + s * kCW;
-      if (c >= l) break;
-      for (int i = lane; i < kw; i += 32)
-        cols[(size_t)s * kw + i] = F32<T>::from(Wat(i, c), scale);
-    }
+  for (int s = warp; s < ncs; s += kCNW) {
+    const int c = rank + s * kCW;
+    if (c >= l) break;
+    for (int i = lane; i < kw; i += 32) cols[(size_t)s * kw + i] = F32<T>::from(Wat(i, c), scale);
   }
   __syncthreads();
 
@@ -268,18 +247,18 @@ __global__ void __launch_bounds__(kCNT, 1)
     }
     if (tid < kCW && tid != rank) cluster.map_shared_rank(ctrl, tid)->tau[par] = ctrl->tau[par];
   };
-  if (!sketch && rank == 0 && warp == 0 && l > 0) {
+  if (rank == 0 && warp == 0 && l > 0) {
     float xn2 = 0.f;
     for (int i = lane; i < kw; i += 32) xn2 += f_abs2(cols[i]);
     xn2 = warp_sum(xn2);
     make_reflector(cols, 0, xn2, refl, &ctrl->tau[0]);
   }
   __syncthreads();
-  if (!sketch && rank == 0 && l > 0) push_reflector(0, 0);
+  if (rank == 0 && l > 0) push_reflector(0, 0);
   cluster.sync();
-  int keff = sketch ? s_rows : kmax;
+  int keff = qsteps;
   float trail = 0.f;
-  for (int j = 0; j < (sketch ? 0 : kmax); ++j) {
+  for (int j = 0; j < qsteps; ++j) {
     const int par = j & 1;
     const F* v = refl + (size_t)par * kw;
     const float tau = ctrl->tau[par];
@@ -347,11 +326,8 @@ __global__ void __launch_bounds__(kCNT, 1)
       if (f < tot) {
         const int half = f / blk, ri = (f % blk) / LP, x = f % LP;
         const int i = (half ? 2 * kCW - 1 - rank : rank) * r + ri;
-        if (sketch) {
-          if (i < keff && x < l) tmp[u] = F32<T>::from(Z[(size_t)i * l + x], scale);
-        } else if (i < keff && x < l && x >= i) {
+        if (i < keff && x < l && x >= i)
           tmp[u] = cluster.map_shared_rank(cols + (size_t)(x / kCW) * kw, x % kCW)[i];
-        }
       }
     }
     cluster.sync();  // column storage is dead from here on
@@ -594,8 +570,7 @@ bool cluster_config(int kw, int l, size_t* smem_out) {
 template <typename T, int E>
 int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw, int l,
                          double thr_rel, double thr_abs, int max_sweeps, T* out_rows,
-                         double* out_nrm, int kcap, JacobiCtl* ctl, double* info, const T* Z,
-                         int s_rows) {
+                         double* out_nrm, int kcap, JacobiCtl* ctl, double* info, int qr_cap) {
   size_t smem = 0;
   if (!cluster_config<T, E>(kw, l, &smem)) {
     set_error("mixed split: cluster configuration not available");
@@ -617,7 +592,7 @@ int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw
   const float tol2 = (float)l * eps * eps;
   SM_CUDA_CHECK(cudaLaunchKernelEx(&cfg, k_split_cluster<T, E>, A, n_a, trans, kw, l, thr_rel,
                                    thr_abs, tol2, max_sweeps, out_rows, out_nrm, kcap, ctl,
-                                   info, Z, s_rows));
+                                   info, qr_cap));
   note_launch();
   return SM_OK;
 }
@@ -656,7 +631,7 @@ bool split_cluster_fits(int kw, int l) {
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, const T* Z, int s_rows) {
+                      JacobiCtl* ctl, double* info, int qr_cap) {
   // W = A^T (kw = n, l = m) when U is wanted, else W = A (kw = m, l = n)
   const int kw = want_u ? n : m;
   const int l = want_u ? m : n;
@@ -665,7 +640,7 @@ int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, do
 #define SM_C(EV)                                                                              \
   case EV:                                                                                    \
     return launch_split_cluster<T, EV>(st, A, n, trans, kw, l, thr_rel, thr_abs, max_sweeps, \
-                                       out_rows, out_nrm, kcap, ctl, info, Z, s_rows)
+                                       out_rows, out_nrm, kcap, ctl, info, qr_cap)
     SM_C(4);
     SM_C(8);
     SM_C(12);
@@ -683,9 +658,8 @@ template bool split_cluster_fits<double>(int, int);
 template bool split_cluster_fits<cplx>(int, int);
 template int split_cluster_f32<double>(cudaStream_t, const double*, int, int, bool, double,
                                        double, int, double*, double*, int, JacobiCtl*, double*,
-                                       const double*, int);
+                                       int);
 template int split_cluster_f32<cplx>(cudaStream_t, const cplx*, int, int, bool, double, double,
-                                     int, cplx*, double*, int, JacobiCtl*, double*, const cplx*,
-                                     int);
+                                     int, cplx*, double*, int, JacobiCtl*, double*, int);
 
 }  // namespace sm

@@ -7,10 +7,12 @@ bond cap) to log2 of the rank the split keeps.  It is trained on the GPU with
 the library's own kernels (``sm_mlp_forward`` / ``sm_mlp_backward`` /
 ``sm_mse_loss`` / ``sm_adam_step``) on truncations that the FP64 method records
 (``sm_rank_features_record``).  Installed with :meth:`RankModel.install` and
-``set_precision("mixed+learned")``, each mixed split replaces its FP32
-rank-revealing QR by a fixed Gaussian sketch of (1.15 predicted rank + 10)
-rows; a split whose sketch missed weight is redone with the QR, and the exact
-discarded weight still sends tolerance violations to the FP64 Jacobi SVD.
+``set_precision("mixed+learned")``, each mixed split stops its FP32
+rank-revealing QR after ceil(1.15 r) + 10 steps (r the predicted rank) instead
+of waiting for the trailing weight to fall below the noise-level threshold; a
+split whose capped QR left weight behind is redone without the cap, and the
+exact discarded weight still sends tolerance violations to the FP64 Jacobi
+SVD.
 
 Input standardisation is folded into the first layer when the model is
 installed, so the device sees raw features.

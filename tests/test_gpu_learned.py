@@ -6,7 +6,7 @@ within 1e-4 of the largest gradient entry, one Adam step within 1e-6, BF16
 inference within 0.05 (relative) of the FP32 network; the trained network's
 mean |error| in log2 rank below the no-network baseline's (the previous
 split's rank); mixed+learned MPO.apply within 1e-10 fidelity of the FP64
-oracle with the sketch in use.
+oracle with the predicted-rank cap in use.
 """
 
 import numpy as np
@@ -145,7 +145,7 @@ def test_mixed_learned_apply_matches_oracle(trained):
                                   "mixed_fallback_sketch", "mixed_fallback_fp32",
                                   "mixed_fallback_cut", "rank_predicted_sum")}
     assert stats["mixed_sketched"] > 5, info
-    # sketches that missed weight are redone with the QR, not counted as FP64 fallbacks
+    # caps that left weight behind are redone without the cap, not counted as FP64 fallbacks
     assert stats["mixed_fallbacks"] <= 0.3 * stats["mixed_sketched"], info
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-10, fe
