@@ -262,7 +262,7 @@ def main():
     ap.add_argument("--form", default="mixed+learned", choices=["plain", "mixed", "mixed+learned"],
                     help="plain = FP64 splits (reference ranks); mixed = FP32 cluster "
                          "factorisation + FP64 refinement; mixed+learned = mixed with the rank "
-                         "predictor sizing a randomized sketch (the metric's headline form)")
+                         "predictor capping the FP32 QR (the metric's headline form)")
     ap.add_argument("--rank-model", default=None,
                     help="trained rank predictor (.npz); trained here when absent")
     ap.add_argument("--train-count", type=int, default=90,
@@ -473,10 +473,10 @@ def main():
                 "cluster_jacobi_ms_per_step": timed_stats["cluster_jacobi_ms"] / k,
                 "fallbacks_coupling_per_step": timed_stats["mixed_fallback_cut"] / k,
                 "fallbacks_fp32_per_step": timed_stats["mixed_fallback_fp32"] / k,
-                "sketched_per_step": timed_stats["mixed_sketched"] / k,
-                "sketch_misses_per_step": timed_stats["mixed_fallback_sketch"] / k,
+                "capped_per_step": timed_stats["mixed_capped"] / k,
+                "cap_redone_per_step": timed_stats["mixed_cap_redone"] / k,
                 "mean_predicted_rank": timed_stats["rank_predicted_sum"]
-                / max(1, timed_stats["mixed_sketched"]),
+                / max(1, timed_stats["mixed_capped"]),
             }
             if learned_info:
                 line["learned"] = learned_info

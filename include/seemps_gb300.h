@@ -274,8 +274,8 @@ typedef struct sm_stats {
   double cluster_jacobi_ms;/* of which: FP32 Jacobi + store (device timer) */
   int64_t mixed_fallback_cut;  /* fallbacks: kept/dropped coupling left after refinement */
   int64_t mixed_fallback_fp32; /* fallbacks: FP32 stage (convergence, resolution, weight) */
-  int64_t mixed_sketched;      /* mixed splits whose QR the predicted rank capped */
-  int64_t mixed_fallback_sketch; /* capped QR left weight: redone without the cap */
+  int64_t mixed_capped;      /* mixed splits whose QR the predicted rank capped */
+  int64_t mixed_cap_redone; /* capped QR left weight: redone without the cap */
   int64_t rank_predicted_sum;  /* predicted kept ranks, summed */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);

@@ -68,8 +68,8 @@ class sm_stats(C.Structure):
         ("cluster_jacobi_ms", C.c_double),
         ("mixed_fallback_cut", C.c_int64),
         ("mixed_fallback_fp32", C.c_int64),
-        ("mixed_sketched", C.c_int64),
-        ("mixed_fallback_sketch", C.c_int64),
+        ("mixed_capped", C.c_int64),
+        ("mixed_cap_redone", C.c_int64),
         ("rank_predicted_sum", C.c_int64),
     ]
 
@@ -261,7 +261,7 @@ PRECISIONS = {"fp64": 0, "mixed": 1, "mixed+learned": 2}
 def set_precision(mode: str, device: int = 0) -> None:
     """Arithmetic of the SVD splits: "fp64" (default, reference ranks), "mixed"
     (FP32 cluster factorisation refined by FP64 GEMMs) or "mixed+learned" (as
-    "mixed", with the installed rank predictor sizing a randomized sketch)."""
+    "mixed", with the installed rank predictor capping the FP32 QR)."""
     if mode not in PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {mode!r}")
     check(load().sm_ctx_set_precision(context(device), PRECISIONS[mode]))

@@ -1335,7 +1335,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
   // a predicted rank caps the rank-revealing QR (qr_cap rows of R)
-  if (qr_cap > 0) ctx.stats.mixed_sketched += 1;
+  if (qr_cap > 0) ctx.stats.mixed_capped += 1;
   SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
                                 info, qr_cap));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
@@ -1468,7 +1468,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
                     r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
   if (missed && !blind && !coupled) {
     // the cap was too small: the caller retries with the uncapped QR
-    ctx.stats.mixed_fallback_sketch += 1;
+    ctx.stats.mixed_cap_redone += 1;
     *missed_out = true;
     return SM_OK;
   }

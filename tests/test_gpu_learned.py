@@ -141,11 +141,11 @@ def test_mixed_learned_apply_matches_oracle(trained):
     finally:
         sg.set_precision("fp64")
     res = so.mpo_apply(mpo, mps, so.DEFAULT_STRATEGY.replace(**kw))
-    info = {k: stats[k] for k in ("mixed_splits", "mixed_sketched", "mixed_fallbacks",
-                                  "mixed_fallback_sketch", "mixed_fallback_fp32",
+    info = {k: stats[k] for k in ("mixed_splits", "mixed_capped", "mixed_fallbacks",
+                                  "mixed_cap_redone", "mixed_fallback_fp32",
                                   "mixed_fallback_cut", "rank_predicted_sum")}
-    assert stats["mixed_sketched"] > 5, info
+    assert stats["mixed_capped"] > 5, info
     # caps that left weight behind are redone without the cap, not counted as FP64 fallbacks
-    assert stats["mixed_fallbacks"] <= 0.3 * stats["mixed_sketched"], info
+    assert stats["mixed_fallbacks"] <= 0.3 * stats["mixed_capped"], info
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-10, fe
