@@ -200,6 +200,7 @@ def workload_config(args):
                         f"+ variational simplify, tol 1e-12, max bond {args.chi}, 2 sweeps",
             "n": args.n, "chi": args.chi, "mpo_bond": 3, "tolerance": 1e-12,
             "max_bond_dimension": args.chi, "sweeps_per_step": 2, "form": args.form,
+            "contractions": getattr(args, "contractions", "fp64"),
             "l2": "flushed between timed steps (256 MB write); the product MPS is >256 MB",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
@@ -263,6 +264,8 @@ def main():
                     help="plain = FP64 splits (reference ranks); mixed = FP32 cluster "
                          "factorisation + FP64 refinement; mixed+learned = mixed with the rank "
                          "predictor capping the FP32 QR (the metric's headline form)")
+    ap.add_argument("--contractions", default="fp64", choices=["fp64", "fp32"],
+                    help="arithmetic of the sweep contractions in the mixed forms")
     ap.add_argument("--rank-model", default=None,
                     help="trained rank predictor (.npz); trained here when absent")
     ap.add_argument("--train-count", type=int, default=90,
@@ -337,7 +340,8 @@ def main():
         psw = sg.state.last_report["sweeps"]
         plain = {"value": psw * len(pt) / (sum(pt) / 1e3), "unit": "sweeps/s",
                  "ms_per_step": sum(pt) / len(pt)}
-    sg.set_precision({"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed+learned"}[args.form])
+    sg.set_precision({"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed+learned"}[args.form],
+                     contractions=args.contractions)
 
     for _ in range(max(3, args.warmup)):
         out = step()

@@ -108,6 +108,11 @@ enum { SM_PRECISION_FP64 = 0, SM_PRECISION_MIXED = 1, SM_PRECISION_MIXED_LEARNED
  * without the cap, and the exact discarded-weight check still sends tolerance
  * violations to the FP64 Jacobi SVD. */
 int sm_ctx_set_precision(void* ctx, int precision);
+/* Arithmetic of the sweep contractions (environments, two-site tensors,
+ * canonical absorptions) in the mixed forms: 64 (default, FP64) or 32 (FP32
+ * arithmetic on FP64 data, ~1e-7 relative error per contraction).  Ignored in
+ * SM_PRECISION_FP64. */
+int sm_ctx_set_contraction_bits(void* ctx, int bits);
 
 /* ---- rank predictor (no reference counterpart) ------------------------------
  * An MLP with GELU hidden layers; parameters are one FP32 device array, layer
@@ -277,6 +282,9 @@ typedef struct sm_stats {
   int64_t mixed_capped;      /* mixed splits whose QR the predicted rank capped */
   int64_t mixed_cap_redone; /* capped QR left weight: redone without the cap */
   int64_t rank_predicted_sum;  /* predicted kept ranks, summed */
+  int64_t gemm32_launches;     /* contractions computed in FP32 (mixed forms) */
+  double gemm32_flops;
+  double gemm32_ms;            /* event-timed (stats timing on) */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

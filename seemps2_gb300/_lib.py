@@ -71,6 +71,9 @@ class sm_stats(C.Structure):
         ("mixed_capped", C.c_int64),
         ("mixed_cap_redone", C.c_int64),
         ("rank_predicted_sum", C.c_int64),
+        ("gemm32_launches", C.c_int64),
+        ("gemm32_flops", C.c_double),
+        ("gemm32_ms", C.c_double),
     ]
 
 
@@ -87,6 +90,7 @@ SIGNATURES = {
     "sm_ctx_create": (C.c_int, [C.POINTER(vp), C.c_int]),
     "sm_ctx_destroy": (C.c_int, [vp]),
     "sm_ctx_set_precision": (C.c_int, [vp, C.c_int]),
+    "sm_ctx_set_contraction_bits": (C.c_int, [vp, C.c_int]),
     "sm_split_rows_f32": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_double,
                                     C.c_double, vp, dp, C.c_int, ip, ip, vp]),
     "sm_truncate": (C.c_int, [vp, vp, C.c_int, stp, ip, dp, vp]),
@@ -258,13 +262,16 @@ class SplitTrace:
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed+learned": 2}
 
 
-def set_precision(mode: str, device: int = 0) -> None:
+def set_precision(mode: str, device: int = 0, contractions: str = "fp64") -> None:
     """Arithmetic of the SVD splits: "fp64" (default, reference ranks), "mixed"
     (FP32 cluster factorisation refined by FP64 GEMMs) or "mixed+learned" (as
     "mixed", with the installed rank predictor capping the FP32 QR)."""
     if mode not in PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {mode!r}")
+    if contractions not in ("fp64", "fp32"):
+        raise ValueError("contractions must be 'fp64' or 'fp32'")
     check(load().sm_ctx_set_precision(context(device), PRECISIONS[mode]))
+    check(load().sm_ctx_set_contraction_bits(context(device), 32 if contractions == "fp32" else 64))
 
 
 def stats_reset(timing: bool = False, device: int = 0):

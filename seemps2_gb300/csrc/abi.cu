@@ -234,6 +234,16 @@ int sm_split_rows_f32(void* ctx, int dtype, const void* A, int m, int n, int wan
   return SM_OK;
 }
 
+int sm_ctx_set_contraction_bits(void* ctx, int bits) {
+  SM_GUARD_CTX(ctx);
+  if (bits != 32 && bits != 64) {
+    set_error("sm_ctx_set_contraction_bits: bits must be 32 or 64");
+    return SM_ERR_VALUE;
+  }
+  as_ctx(ctx)->contract32 = bits == 32;
+  return SM_OK;
+}
+
 int sm_truncate(void* ctx, const double* s_dev, int n, const sm_strategy* st, int* rank,
                 double* err2, void* stream) {
   SM_GUARD_CTX(ctx);

@@ -143,6 +143,111 @@ __global__ void k_splitk_reduce(int M, int N, int nz, const T* __restrict__ part
   }
 }
 
+// ---- FP32-arithmetic variant (contractions of the mixed forms) --------------
+// Same tiling as k_gemm; operands are rounded to FP32 (complex: two FP32) when
+// staged in shared memory and the products accumulate in FP32; alpha, beta
+// and the output stay FP64.  Relative error ~1e-7 |A||B| per entry.
+template <typename T> struct C32;
+template <> struct C32<double> {
+  using type = float;
+  __device__ static float from(double x) { return (float)x; }
+  __device__ static double to(float x) { return (double)x; }
+  __device__ static float zero() { return 0.f; }
+  __device__ static float fma(float a, float b, float c) { return fmaf(a, b, c); }
+};
+template <> struct C32<cplx> {
+  using type = float2;
+  __device__ static float2 from(cplx x) { return make_float2((float)x.re, (float)x.im); }
+  __device__ static cplx to(float2 x) { return cplx{(double)x.x, (double)x.y}; }
+  __device__ static float2 zero() { return make_float2(0.f, 0.f); }
+  __device__ static float2 fma(float2 a, float2 b, float2 c) {
+    return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_gemm32(int opA, int opB, int M, int N, int K, T alpha,
+                                               const T* __restrict__ A, int lda,
+                                               const T* __restrict__ B, int ldb, T beta,
+                                               T* __restrict__ C, int ldc, int kchunk,
+                                               T* __restrict__ part) {
+  using F = typename C32<T>::type;
+  __shared__ F As[BK][BM + 1];
+  __shared__ F Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  F acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = C32<T>::zero();
+  const int kbeg = blockIdx.z * kchunk;
+  const int kend = min(K, kbeg + kchunk);
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+    for (int e = 0; e < (BM * BK) / NT; ++e) {
+      const int idx = tid + e * NT;
+      int mm, kk;
+      if (opA == SM_OP_N) { mm = idx / BK; kk = idx % BK; }
+      else                { kk = idx / BM; mm = idx % BM; }
+      const int gm = m0 + mm, gk = k0 + kk;
+      T v = S<T>::zero();
+      if (gm < M && gk < kend)
+        v = opA == SM_OP_N ? load_op(A + (size_t)gm * lda + gk, opA)
+                           : load_op(A + (size_t)gk * lda + gm, opA);
+      As[kk][mm] = C32<T>::from(v);
+    }
+#pragma unroll
+    for (int e = 0; e < (BN * BK) / NT; ++e) {
+      const int idx = tid + e * NT;
+      int nn, kk;
+      if (opB == SM_OP_N) { kk = idx / BN; nn = idx % BN; }
+      else                { nn = idx / BK; kk = idx % BK; }
+      const int gn = n0 + nn, gk = k0 + kk;
+      T v = S<T>::zero();
+      if (gn < N && gk < kend)
+        v = opB == SM_OP_N ? load_op(B + (size_t)gk * ldb + gn, opB)
+                           : load_op(B + (size_t)gn * ldb + gk, opB);
+      Bs[kk][nn] = C32<T>::from(v);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      F a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = C32<T>::fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  const bool use_beta = S<T>::abs2(beta) != 0.0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + tx + 16 * j;
+      if (gn >= N) continue;
+      const T r = C32<T>::to(acc[i][j]);
+      if (part) {
+        part[(size_t)blockIdx.z * M * N + (size_t)gm * N + gn] = r;
+      } else {
+        T* c = C + (size_t)gm * ldc + gn;
+        T v = alpha * r;
+        if (use_beta) v = S<T>::fma(beta, *c, v);
+        *c = v;
+      }
+    }
+  }
+}
+
 }  // namespace
 
 template <typename T>
@@ -222,6 +327,50 @@ int gemm_ctx(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T
   ctx.stats.gemm_ms += ms;
   return SM_OK;
 }
+
+template <typename T>
+int gemm_ctx_f32(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha,
+                 const T* A, int lda, const T* B, int ldb, T beta, T* C, int ldc) {
+  if (M == 0 || N == 0 || K == 0) return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  ctx.stats.gemm32_launches += 1;
+  ctx.stats.gemm32_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
+  // FP32 runs 64x the FP64 rate: split K only when the output has very few tiles
+  const int nz = splitk_slices(M, N, K, std::max(1, ctx.num_sms) / 2);
+  T* part = nullptr;
+  if (nz > 1) SM_CHECK(ctx.scratch("gemm.splitk", (size_t)nz * M * N, &part));
+  const int kchunk = nz > 1 ? ((K + nz - 1) / nz + BK - 1) / BK * BK : K;
+  const int nzz = nz > 1 ? (K + kchunk - 1) / kchunk : 1;
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, nzz);
+  if (grid.y > 65535) {
+    set_error("gemm: M too large");
+    return SM_ERR_VALUE;
+  }
+  if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+  k_gemm32<T><<<grid, NT, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kchunk,
+                                   nzz > 1 ? part : nullptr);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  if (nzz > 1) {
+    const size_t mn = (size_t)M * N;
+    const int blocks = (int)std::min<size_t>((mn + 255) / 256, 4096);
+    k_splitk_reduce<T><<<blocks, 256, 0, st>>>(M, N, nzz, part, alpha, beta, C, ldc);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+  }
+  if (ctx.timing) {
+    SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+    SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
+    float ms = 0.f;
+    SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+    ctx.stats.gemm32_ms += ms;
+  }
+  return SM_OK;
+}
+
+template int gemm_ctx_f32<double>(Ctx&, cudaStream_t, int, int, int, int, int, double,
+                                  const double*, int, const double*, int, double, double*, int);
+template int gemm_ctx_f32<cplx>(Ctx&, cudaStream_t, int, int, int, int, int, cplx, const cplx*,
+                                int, const cplx*, int, cplx, cplx*, int);
 
 template int gemm_ctx<double>(Ctx&, cudaStream_t, int, int, int, int, int, double, const double*,
                               int, const double*, int, double, double*, int);

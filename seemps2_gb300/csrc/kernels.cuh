@@ -31,6 +31,7 @@ struct Ctx {
   // rank features: position of the split being made (set by the sweep
   // driver), the previous split's kept rank and leading singular values,
   // the model, and the recorder (features, kept rank) of every split
+  bool contract32 = false;  // mixed forms: sweep contractions in FP32 arithmetic
   int split_site = -1, split_n = 0;
   int prev_rank = 0;
   std::vector<double> prev_s;
@@ -98,6 +99,11 @@ int gemm_ctx(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T
 template <typename T>
 int gemm(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda,
          const T* B, int ldb, T beta, T* C, int ldc);
+// Same contract with FP32 arithmetic (FP64 operands rounded on load, FP32
+// accumulation): the contractions of the mixed forms.
+template <typename T>
+int gemm_ctx_f32(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha,
+                 const T* A, int lda, const T* B, int ldb, T beta, T* C, int ldc);
 
 // --- mps_ops.cu ------------------------------------------------------------
 template <typename T>

@@ -71,6 +71,8 @@ struct Sweeper {
   // ---- helpers -------------------------------------------------------------
   int gemm_(int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda, const T* B,
             int ldb, T beta, T* C, int ldc) {
+    if (ctx.precision != SM_PRECISION_FP64 && ctx.contract32)
+      return gemm_ctx_f32<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
     return gemm_ctx<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   }
   static T one() { return S<T>::one(); }
