@@ -75,6 +75,11 @@ struct Sweeper {
       return gemm_ctx_f32<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
     return gemm_ctx<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   }
+  // FP64 contractions whatever the context's setting (norms and overlaps)
+  int gemm64_(int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda, const T* B,
+              int ldb, T beta, T* C, int ldc) {
+    return gemm_ctx<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  }
   static T one() { return S<T>::one(); }
   static T zero() { return S<T>::zero(); }
 
@@ -170,10 +175,10 @@ struct Sweeper {
     SM_CHECK(set_identity<T>(st, 1, rho, 1));
     for (int i = 0; i < L; ++i) {
       // t = rho (ab[i] x bb[i]) @ B[i] (bb[i] x d*bb[i+1])
-      SM_CHECK(gemm_(SM_OP_N, SM_OP_N, ab[i], d[i] * bbnd[i + 1], bbnd[i], one(), rho, bbnd[i], B[i],
+      SM_CHECK(gemm64_(SM_OP_N, SM_OP_N, ab[i], d[i] * bbnd[i + 1], bbnd[i], one(), rho, bbnd[i], B[i],
                      d[i] * bbnd[i + 1], zero(), t, d[i] * bbnd[i + 1]));
       // rho' = A[i]^H (ab[i+1] x ab[i]*d) @ t (ab[i]*d x bb[i+1])
-      SM_CHECK(gemm_(SM_OP_C, SM_OP_N, ab[i + 1], bbnd[i + 1], ab[i] * d[i], one(), A[i], ab[i + 1], t,
+      SM_CHECK(gemm64_(SM_OP_C, SM_OP_N, ab[i + 1], bbnd[i + 1], ab[i] * d[i], one(), A[i], ab[i + 1], t,
                      bbnd[i + 1], zero(), rho2, bbnd[i + 1]));
       std::swap(rho, rho2);
     }
@@ -469,6 +474,18 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
       rep->sweeps = sweep + 1;
       if (err < s.simplification_tolerance || err > old_err) break;
       dir = -dir;
+    }
+    if (ctx.contract32 && ctx.precision != SM_PRECISION_FP64) {
+      // the error bound's last term needs the overlap to FP64 accuracy: rebuild
+      // the environments of the final centre with FP64 contractions
+      ctx.contract32 = false;
+      const int rc = w.init_environments(c);
+      double sc = 0.0;
+      const int rc2 = rc == SM_OK ? w.estimate(c, &nm, &sc) : rc;
+      ctx.contract32 = true;
+      SM_CHECK(rc2);
+      err = 2.0 * std::fabs(1.0 - sc / std::sqrt(nm * norm_state_sqr));
+      if (rep->sweeps >= 1 && rep->sweeps <= 64) rep->sweep_err[rep->sweeps - 1] = err;
     }
     double state_error = 0.0;
     for (int t = 0; t < w.nt; ++t) state_error += w.wabs[t] * w.term_err[t];
