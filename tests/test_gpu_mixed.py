@@ -251,3 +251,27 @@ def test_mixed_apply_random_complex(mixed):
     assert _lib.stats_read()["mixed_splits"] > 5
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-10, fe
+
+
+def test_mixed_fp32_contractions_apply():
+    """Mixed splits with FP32-arithmetic contractions (tol 1e-12, max bond chi,
+    2 sweeps): fidelity error below 1e-10 against the FP64 oracle.  The error
+    bound (a sum of sqrt(discarded weight) over all splits, which magnifies
+    1e-7-level differences of tiny discarded weights) agrees to 1e-4 relative;
+    the state norm and the final sweep estimate stay FP64."""
+    n, chi = 14, 64
+    mps, mpo = laplacian_case(n, chi)
+    kw = dict(tolerance=1e-12, max_bond_dimension=chi, max_sweeps=2, simplification_tolerance=0.0)
+    st = sg.DEFAULT_STRATEGY.replace(**kw)
+    sg.set_precision("mixed", contractions="fp32")
+    _lib.stats_reset()
+    try:
+        out = sg.MPO(mpo, st).apply(sg.MPS(mps), strategy=st)
+        stats = _lib.stats_read()
+    finally:
+        sg.set_precision("fp64")
+    res = so.mpo_apply(mpo, mps, so.DEFAULT_STRATEGY.replace(**kw))
+    assert stats["gemm32_launches"] > 50
+    fe = so.fidelity_error(mps_np(out), res.tensors)
+    assert fe < 1e-10, fe
+    assert abs(out.error() - res.error) <= 1e-4 * res.error + 1e-12, (out.error(), res.error)
