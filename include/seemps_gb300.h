@@ -242,6 +242,31 @@ int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms,
                 const int64_t* out_cap, int* out_bonds, sm_simplify_report* rep,
                 void* stream);
 
+/* sm_simplify with the terms' products given: gram holds nterms*nterms
+ * complex pairs, gram[2*(i*nterms+j)] + 1j*gram[2*(i*nterms+j)+1] = <psi_i|psi_j>,
+ * used where the reference takes scprod of the terms for the state norm
+ * (state/simplification.py:101 for one state, delete_zero_components at
+ * :176 for sums).  MPO.apply (operators/mpo.py:229-281) fills it from
+ * sm_mpo_scprod, so the norm of the bond-(chi*D) product is never contracted.
+ * Results equal sm_simplify's to FP64 rounding of the norm. */
+int sm_simplify_gram(void* ctx, int dtype, int L, const int* phys, int nterms,
+                     const double* weights, const int* ket_bonds,
+                     const void* const* ket_sites, const double* term_errors,
+                     const double* gram, const sm_strategy* st, int direction,
+                     void* const* out_sites, const int64_t* out_cap, int* out_bonds,
+                     sm_simplify_report* rep, void* stream);
+
+/* <O bra|O ket> for an MPO O (site i: mpo_bonds[i] x dout[i] x din[i] x
+ * mpo_bonds[i+1]) and two MPS with physical dimensions din: the scprod
+ * (cython/environments.pxi:87-118) of the products O|bra>, O|ket>
+ * (_mpo_multiply_tensor, operators/mpo.py:26-45) computed from the factors
+ * with environments E[x, alpha, beta, y], 4 d D^2 chi^3 flops per site instead
+ * of 4 d (D chi)^3.  out[0] (+ out[1] for complex) as for sm_scprod. */
+int sm_mpo_scprod(void* ctx, int dtype, int L, const int* dout, const int* din,
+                  const int* mpo_bonds, const void* const* mpo, const int* bra_bonds,
+                  const void* const* bra, const int* ket_bonds, const void* const* ket,
+                  double* out, void* stream);
+
 /* Upper bound on the bond dimensions a simplify of these kets can produce:
  * min(max_bond_dimension, summed ket bond); fills cap_bonds (L+1). */
 int sm_simplify_bond_caps(int L, const int* phys, int nterms, const int* ket_bonds,

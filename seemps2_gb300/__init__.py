@@ -27,7 +27,7 @@ from .core import (
     destructively_truncate_vector,
 )
 from ._lib import set_precision
-from .operators import MPO, MPOList
+from .operators import MPO, MPOList, mpo_scprod
 from .state import (
     SIMPLIFICATION_STRATEGY,
     CanonicalMPS,
@@ -46,5 +46,5 @@ __all__ = [
     "DEFAULT_STRATEGY", "DEFAULT_TOLERANCE", "MAX_BOND_DIMENSION", "NO_TRUNCATION", "GemmOrder",
     "Simplification", "Strategy", "Truncation", "destructively_truncate_vector", "MPO", "MPOList",
     "SIMPLIFICATION_STRATEGY", "CanonicalMPS", "MPS", "MPSSum", "random_mps", "random_uniform_mps",
-    "scprod", "simplify", "simplify_mps", "simplify_mps_sum", "vdot", "set_precision",
+    "scprod", "simplify", "simplify_mps", "simplify_mps_sum", "vdot", "set_precision", "mpo_scprod",
 ]

@@ -114,6 +114,11 @@ SIGNATURES = {
                                   dp, vp]),
     "sm_simplify": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, dp, ip, C.POINTER(vp), dp, stp,
                               C.c_int, C.POINTER(vp), i64p, ip, C.POINTER(sm_simplify_report), vp]),
+    "sm_simplify_gram": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, dp, ip, C.POINTER(vp), dp,
+                                   dp, stp, C.c_int, C.POINTER(vp), i64p, ip,
+                                   C.POINTER(sm_simplify_report), vp]),
+    "sm_mpo_scprod": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, ip, C.POINTER(vp), ip, C.POINTER(vp),
+                                ip, C.POINTER(vp), dp, vp]),
     "sm_simplify_bond_caps": (C.c_int, [C.c_int, ip, C.c_int, ip, stp, ip]),
     "sm_trace_enable": (C.c_int, [vp, C.c_int]),
     "sm_trace_read": (C.c_int, [vp, ip, i64p, ip, ip, dp, dp]),

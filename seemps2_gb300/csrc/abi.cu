@@ -11,7 +11,11 @@ namespace sm {
 template <typename T>
 int simplify_impl(Ctx&, cudaStream_t, int, const int*, int, const double*, const double*,
                   const int*, const void* const*, const sm_strategy&, int, void* const*,
-                  const int64_t*, int*, sm_simplify_report*);
+                  const int64_t*, int*, sm_simplify_report*, const double*);
+template <typename T>
+int mpo_scprod_impl(Ctx&, cudaStream_t, int, const int*, const int*, const int*,
+                    const void* const*, const int*, const void* const*, const int*,
+                    const void* const*, double*);
 template <typename T>
 int canonicalize_impl(Ctx&, cudaStream_t, int, const int*, int*, void* const*, const int64_t*,
                       int, const sm_strategy&, double*);
@@ -388,10 +392,11 @@ int sm_canonicalize(void* ctx, int dtype, int L, const int* phys, int* bonds, vo
                                  center, *st, err);
 }
 
-int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms, const double* weights,
-                const int* ket_bonds, const void* const* ket_sites, const double* term_errors,
-                const sm_strategy* st, int direction, void* const* out_sites,
-                const int64_t* out_cap, int* out_bonds, sm_simplify_report* rep, void* stream) {
+static int simplify_entry(void* ctx, int dtype, int L, const int* phys, int nterms,
+                          const double* weights, const int* ket_bonds, const void* const* ket_sites,
+                          const double* term_errors, const sm_strategy* st, int direction,
+                          void* const* out_sites, const int64_t* out_cap, int* out_bonds,
+                          sm_simplify_report* rep, const double* gram, void* stream) {
   SM_GUARD_CTX(ctx);
   SM_CHECK(check_dtype(dtype));
   SM_CHECK(check_strategy(st));
@@ -414,10 +419,60 @@ int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms, const 
   if (dtype == SM_FLOAT64)
     return simplify_impl<double>(*as_ctx(ctx), as_stream(stream), L, phys, nterms, weights,
                                  term_errors, ket_bonds, ket_sites, *st, direction, out_sites,
-                                 out_cap, out_bonds, rep);
+                                 out_cap, out_bonds, rep, gram);
   return simplify_impl<cplx>(*as_ctx(ctx), as_stream(stream), L, phys, nterms, weights,
                              term_errors, ket_bonds, ket_sites, *st, direction, out_sites, out_cap,
-                             out_bonds, rep);
+                             out_bonds, rep, gram);
+}
+
+int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms, const double* weights,
+                const int* ket_bonds, const void* const* ket_sites, const double* term_errors,
+                const sm_strategy* st, int direction, void* const* out_sites,
+                const int64_t* out_cap, int* out_bonds, sm_simplify_report* rep, void* stream) {
+  return simplify_entry(ctx, dtype, L, phys, nterms, weights, ket_bonds, ket_sites, term_errors, st,
+                        direction, out_sites, out_cap, out_bonds, rep, nullptr, stream);
+}
+
+int sm_simplify_gram(void* ctx, int dtype, int L, const int* phys, int nterms,
+                     const double* weights, const int* ket_bonds, const void* const* ket_sites,
+                     const double* term_errors, const double* gram, const sm_strategy* st,
+                     int direction, void* const* out_sites, const int64_t* out_cap, int* out_bonds,
+                     sm_simplify_report* rep, void* stream) {
+  if (!gram) {
+    set_error("simplify_gram: gram must not be null");
+    return SM_ERR_VALUE;
+  }
+  return simplify_entry(ctx, dtype, L, phys, nterms, weights, ket_bonds, ket_sites, term_errors, st,
+                        direction, out_sites, out_cap, out_bonds, rep, gram, stream);
+}
+
+int sm_mpo_scprod(void* ctx, int dtype, int L, const int* dout, const int* din,
+                  const int* mpo_bonds, const void* const* mpo, const int* bra_bonds,
+                  const void* const* bra, const int* ket_bonds, const void* const* ket,
+                  double* out, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (L < 1 || !dout || !din || !mpo_bonds || !mpo || !bra_bonds || !bra || !ket_bonds || !ket ||
+      !out) {
+    set_error("mpo_scprod: need L >= 1 and non-null arguments");
+    return SM_ERR_VALUE;
+  }
+  for (int i = 0; i <= L; ++i)
+    if (mpo_bonds[i] <= 0 || bra_bonds[i] <= 0 || ket_bonds[i] <= 0 ||
+        (i < L && (dout[i] <= 0 || din[i] <= 0))) {
+      set_error("mpo_scprod: non-positive dimension");
+      return SM_ERR_VALUE;
+    }
+  if (mpo_bonds[0] != 1 || mpo_bonds[L] != 1 || bra_bonds[0] != 1 || bra_bonds[L] != 1 ||
+      ket_bonds[0] != 1 || ket_bonds[L] != 1) {
+    set_error("mpo_scprod: open boundary bonds must be 1");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return mpo_scprod_impl<double>(*as_ctx(ctx), as_stream(stream), L, dout, din, mpo_bonds, mpo,
+                                   bra_bonds, bra, ket_bonds, ket, out);
+  return mpo_scprod_impl<cplx>(*as_ctx(ctx), as_stream(stream), L, dout, din, mpo_bonds, mpo,
+                               bra_bonds, bra, ket_bonds, ket, out);
 }
 
 int sm_simplify_bond_caps(int L, const int* phys, int nterms, const int* ket_bonds,

@@ -293,7 +293,7 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
                   const double* weights, const double* term_errors, const int* ket_bonds,
                   const void* const* ket_sites, const sm_strategy& s, int direction,
                   void* const* out_sites, const int64_t* out_cap, int* out_bonds,
-                  sm_simplify_report* rep) {
+                  sm_simplify_report* rep, const double* gram) {
   Sweeper<T> S_(ctx, st, s);
   auto& w = S_;
   w.L = L;
@@ -310,18 +310,28 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
       kbs[t].assign(ket_bonds + (size_t)t * (L + 1), ket_bonds + (size_t)(t + 1) * (L + 1));
     }
     // a plain MPS is the one-term sum with weight 1: |w|^2 |<s|s>| is then
-    // exactly the reference's abs(scprod(state, state).real)
+    // exactly the reference's abs(scprod(state, state).real).  A caller that
+    // knows the terms' products (the MPO apply, from the factors) passes them
+    // as `gram` (<s_i|s_j>, row-major complex pairs) instead.
+    auto product = [&](int i, int j, double* v) -> int {
+      if (gram) {
+        v[0] = gram[2 * ((size_t)i * nterms + j)];
+        v[1] = gram[2 * ((size_t)i * nterms + j) + 1];
+        return SM_OK;
+      }
+      return w.scprod(kets[i], kbs[i], kets[j], kbs[j], v);
+    };
     double c = 0.0;
     for (int i = 0; i < nterms; ++i) {
       const double* wi = weights + 2 * i;
       double sc[2];
-      SM_CHECK(w.scprod(kets[i], kbs[i], kets[i], kbs[i], sc));
+      SM_CHECK(product(i, i, sc));
       const double ni = (wi[0] * wi[0] + wi[1] * wi[1]) * std::fabs(sc[0]);
       if (ni) {
         for (int j : keep) {
           const double* wj = weights + 2 * j;
           double p[2];
-          SM_CHECK(w.scprod(kets[i], kbs[i], kets[j], kbs[j], p));
+          SM_CHECK(product(i, j, p));
           // (conj(wi) wj <s_i|s_j>).real
           const double ar = wi[0] * wj[0] + wi[1] * wj[1];
           const double ai = wi[0] * wj[1] - wi[1] * wj[0];
@@ -559,7 +569,7 @@ int scprod_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, const int* ab
   template int simplify_impl<T>(Ctx&, cudaStream_t, int, const int*, int, const double*,       \
                                 const double*, const int*, const void* const*,                 \
                                 const sm_strategy&, int, void* const*, const int64_t*, int*,   \
-                                sm_simplify_report*);                                          \
+                                sm_simplify_report*, const double*);                           \
   template int canonicalize_impl<T>(Ctx&, cudaStream_t, int, const int*, int*, void* const*,   \
                                     const int64_t*, int, const sm_strategy&, double*);         \
   template int scprod_impl<T>(Ctx&, cudaStream_t, int, const int*, const int*,                 \

@@ -2,10 +2,13 @@
 
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 
+from . import _lib
 from .core import DEFAULT_STRATEGY, Strategy, _mpo_multiply_tensor, as_device
-from .state import MPS, MPSSum, TensorArray, simplify
+from .state import MPS, MPSSum, TensorArray, _simplify_terms, simplify
 
 
 class MPO(TensorArray):
@@ -81,7 +84,8 @@ class MPO(TensorArray):
             if self.size != state.size:
                 raise ValueError("MPO and state must have the same size")
             out = None
-            for i, (w, mps) in enumerate(zip(state.weights, state.states)):
+            factors = list(zip(state.weights, state.states))
+            for i, (w, mps) in enumerate(factors):
                 Ostate = w * MPS([_mpo_multiply_tensor(A, B) for A, B in zip(self._data, mps._data)],
                                  error=mps.error())
                 out = Ostate if i == 0 else out + Ostate
@@ -89,12 +93,18 @@ class MPO(TensorArray):
         elif isinstance(state, MPS):
             if self.size != state.size:
                 raise ValueError("MPO and state must have the same size")
+            factors = [(1.0, state)]
             state = MPS([_mpo_multiply_tensor(A, B) for A, B in zip(self._data, state._data)],
                         error=state.error())
         else:
             raise TypeError(f"Cannot multiply MPO with {state}")
         if simplify:
-            state = _simplify(state, strategy=strategy)
+            # the products' norms and overlaps come from the factors
+            # (sm_mpo_scprod) instead of the bond-(chi D) product states
+            terms = state.states if isinstance(state, MPSSum) else [state]
+            weights = state.weights if isinstance(state, MPSSum) else [1.0]
+            gram = _product_gram(self._data, factors) if len(terms) == len(factors) else None
+            state = _simplify_terms(weights, terms, strategy, +1, gram=gram)
         return state
 
     def __matmul__(self, b):
@@ -113,6 +123,47 @@ class MPO(TensorArray):
 
 
 _simplify = simplify
+
+
+def mpo_scprod(mpo: MPO, bra: MPS, ket: MPS):
+    """<O bra|O ket> from the factors, without forming the products
+    (the scprod of cython/environments.pxi:87-118 applied to O|bra>, O|ket>)."""
+    return _mpo_scprod(mpo._data, bra, ket)
+
+
+def _mpo_scprod(data, bra: MPS, ket: MPS):
+    if not (len(data) == bra.size == ket.size):
+        raise ValueError("Invalid arguments to mpo_scprod")
+    cplx = (bra.is_complex() or ket.is_complex() or
+            any((t.is_complex() if hasattr(t, "is_complex") else np.iscomplexobj(t)) for t in data))
+    O = [as_device(t, cplx) for t in data]
+    A = [as_device(t, cplx) for t in bra._data]
+    B = [as_device(t, cplx) for t in ket._data]
+    out = (C.c_double * 2)()
+    _lib.check(_lib.load().sm_mpo_scprod(
+        _lib.context(), _lib.SM_COMPLEX128 if cplx else _lib.SM_FLOAT64, len(O),
+        _lib.int_array([t.shape[1] for t in O]), _lib.int_array([t.shape[2] for t in O]),
+        _lib.int_array([O[0].shape[0]] + [t.shape[3] for t in O]), _lib.ptr_array(O),
+        _lib.int_array(bra.bond_dimensions()), _lib.ptr_array(A),
+        _lib.int_array(ket.bond_dimensions()), _lib.ptr_array(B), out, _lib.stream_handle()))
+    return complex(out[0], out[1]) if cplx else out[0]
+
+
+def _product_gram(data, factors):
+    """<w_i O s_i|w_j O s_j> for the terms (w_i, s_i) of an MPO apply, as the
+    nterms x nterms complex array sm_simplify_gram takes."""
+    n = len(factors)
+    G = np.zeros((n, n), dtype=complex)
+    for i in range(n):
+        for j in range(i, n):
+            wi, si = factors[i]
+            wj, sj = factors[j]
+            v = np.conj(complex(wi)) * complex(wj)
+            if v != 0:
+                v *= complex(_mpo_scprod(data, si, sj))
+            G[i, j] = v
+            G[j, i] = np.conj(v)
+    return G
 
 
 class MPOList:

@@ -446,7 +446,10 @@ SIMPLIFICATION_STRATEGY = Strategy(method=Truncation.RELATIVE_NORM_SQUARED_ERROR
 last_report: dict = {}
 
 
-def _simplify_terms(weights, states, strategy: Strategy, direction: int) -> CanonicalMPS:
+def _simplify_terms(weights, states, strategy: Strategy, direction: int,
+                    gram=None) -> CanonicalMPS:
+    """simplify of sum_t w_t |s_t>; `gram` (optional, nterms x nterms complex,
+    <s_i|s_j>) replaces the terms' scprods in the state norm."""
     torch = _torch()
     cplx = any(isinstance(w, complex) and w.imag != 0 for w in weights) or any(s.is_complex() for s in states)
     states = [s if (s.is_complex() == cplx) else MPS(s._data, s._error) for s in states]
@@ -468,12 +471,17 @@ def _simplify_terms(weights, states, strategy: Strategy, direction: int) -> Cano
     out_bonds = (C.c_int * (L + 1))()
     rep = _lib.sm_simplify_report()
     flat = [t for k in kets for t in k]
-    _lib.check(_lib.load().sm_simplify(
-        _lib.context(), _lib.SM_COMPLEX128 if cplx else _lib.SM_FLOAT64, L, _lib.int_array(phys),
-        nterms, _lib.dbl_array(wpairs), _lib.int_array(bonds), _lib.ptr_array(flat),
-        _lib.dbl_array([s._error for s in states]), C.byref(st_c), int(direction),
-        _lib.ptr_array(outs), _lib.i64_array([o.numel() for o in outs]), out_bonds,
-        C.byref(rep), _lib.stream_handle()))
+    head = (_lib.context(), _lib.SM_COMPLEX128 if cplx else _lib.SM_FLOAT64, L,
+            _lib.int_array(phys), nterms, _lib.dbl_array(wpairs), _lib.int_array(bonds),
+            _lib.ptr_array(flat), _lib.dbl_array([s._error for s in states]))
+    tail = (C.byref(st_c), int(direction), _lib.ptr_array(outs),
+            _lib.i64_array([o.numel() for o in outs]), out_bonds, C.byref(rep), _lib.stream_handle())
+    if gram is None:
+        _lib.check(_lib.load().sm_simplify(*head, *tail))
+    else:
+        g = np.asarray(gram, dtype=complex).reshape(nterms, nterms)
+        pairs = np.stack([g.real, g.imag], axis=-1).reshape(-1)
+        _lib.check(_lib.load().sm_simplify_gram(*head, _lib.dbl_array(pairs.tolist()), *tail))
     data = [outs[i][: out_bonds[i] * phys[i] * out_bonds[i + 1]].view(out_bonds[i], phys[i],
                                                                          out_bonds[i + 1])
             for i in range(L)]
