@@ -497,14 +497,28 @@ __global__ void k_truncate(const double* s, int N, sm_strategy st, double* error
   }
 }
 
-// Sort the k norms descending (stable by index), then truncate.
-__global__ void k_sort_truncate(const double* nrm, int k, sm_strategy st, int* perm,
-                                double* s_sorted, double* errors, const JacobiCtl* ctl,
-                                SplitResult* res) {
-  extern __shared__ unsigned long long keys[];
-  for (int i = threadIdx.x; i < k; i += blockDim.x)
-    keys[i] = (unsigned long long)__double_as_longlong(nrm[i]);
-  __syncthreads();
+// Mixed-form bookkeeping on the sorted values s (cnt of them) and the kept
+// rank D: the discarded weight |A|^2 - sum_{j<D} s_j^2 into res->err2,
+// info[2] = s[0], info[3] = s[D-1] for the host's checks and info[7] =
+// |A|^2 - sum of all cnt values^2, the weight outside the rows' span (what a
+// capped QR left behind).  |A|^2 is info[0].  One thread.
+__device__ void mixed_info(const double* s, int cnt, int D, SplitResult* res, double* info) {
+  double kept_D = 0.0, kept_all = 0.0;
+  for (int j = 0; j < cnt; ++j) {
+    if (j == D) kept_D = kept_all;
+    kept_all += s[j] * s[j];
+  }
+  if (D >= cnt) kept_D = kept_all;
+  res->err2 = fmax(0.0, info[0] - kept_D);
+  info[2] = s[0];
+  info[3] = s[max(D, 1) - 1];
+  info[7] = fmax(0.0, info[0] - kept_all);
+}
+
+// Rank sort of the k non-negative keys (descending, stable by index) by k
+// threads; writes perm, s_sorted (global) and ss (shared, may alias).
+__device__ void rank_sort(const unsigned long long* keys, int k, int* perm, double* s_sorted,
+                          double* ss) {
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     const unsigned long long ki = keys[i];
     int rank = 0;
@@ -513,21 +527,68 @@ __global__ void k_sort_truncate(const double* nrm, int k, sm_strategy st, int* p
       rank += (kj > ki) || (kj == ki && j < i);
     }
     perm[rank] = i;
-    s_sorted[rank] = __longlong_as_double((long long)ki);
+    const double v = __longlong_as_double((long long)ki);
+    s_sorted[rank] = v;
+    ss[rank] = v;
   }
+}
+
+// Sort the k norms descending (stable by index), then truncate.  With
+// `staged` the sorted values and the error table live in shared memory while
+// the one-thread truncation rule runs over them (dynamic shared memory
+// 24 k + 8 bytes instead of 8 k); `info` (optional) also gets mixed_info.
+__global__ void k_sort_truncate(const double* nrm, int k, sm_strategy st, int* perm,
+                                double* s_sorted, double* errors, const JacobiCtl* ctl,
+                                SplitResult* res, int staged, double* info) {
+  extern __shared__ unsigned long long keys[];
+  double* ss = staged ? reinterpret_cast<double*>(keys + k) : s_sorted;
+  double* er = staged ? ss + k : errors;
+  for (int i = threadIdx.x; i < k; i += blockDim.x)
+    keys[i] = (unsigned long long)__double_as_longlong(nrm[i]);
+  __syncthreads();
+  rank_sort(keys, k, perm, s_sorted, ss);
   __syncthreads();
   if (threadIdx.x == 0) {
     int D;
     double e;
-    truncate_rule(s_sorted, k, st, errors, &D, &e);
+    truncate_rule(ss, k, st, er, &D, &e);
     res->D = D;
     res->err2 = e;
     res->status = ctl ? ctl->status : 0;
     res->sweeps = ctl ? ctl->sweeps : 0;
     // non-finite input shows up as a NaN norm
     for (int i = 0; i < k; ++i)
-      if (!(s_sorted[i] == s_sorted[i]) || s_sorted[i] > DBL_MAX) res->status |= DEV_NONFINITE;
+      if (!(ss[i] == ss[i]) || ss[i] > DBL_MAX) res->status |= DEV_NONFINITE;
+    if (info) mixed_info(ss, k, D, res, info);
   }
+  if (staged) {
+    __syncthreads();
+    for (int i = threadIdx.x; i <= k; i += blockDim.x) errors[i] = er[i];
+  }
+}
+
+// Launches k_sort_truncate (one CTA of 1024 threads), staging in shared
+// memory when 24 k + 8 bytes fit.
+static int sort_truncate(cudaStream_t st, const double* nrm, int k, const sm_strategy& strat,
+                         int* perm, double* s_sorted, double* errors, const JacobiCtl* ctl,
+                         SplitResult* res, double* info = nullptr) {
+  constexpr size_t kLimit = 200 * 1024;
+  const size_t keys = sizeof(unsigned long long) * (size_t)k;
+  const size_t full = keys + sizeof(double) * (2 * (size_t)k + 1);
+  const bool staged = full <= kLimit;
+  const size_t smem = staged ? full : keys;
+  if (smem > kLimit) {
+    set_error("svd: matrix too large for the on-chip sort");
+    return SM_ERR_VALUE;
+  }
+  if (smem > 48 * 1024)
+    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+  k_sort_truncate<<<1, 1024, smem, st>>>(nrm, k, strat, perm, s_sorted, errors, ctl, res,
+                                         staged ? 1 : 0, info);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
 }
 
 // Write the factors of the truncated SVD.  Element (i, j) of the left output
@@ -949,17 +1010,7 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
-  const size_t smem = sizeof(unsigned long long) * (size_t)k;
-  if (smem > 200 * 1024) {
-    set_error("svd: matrix too large for the on-chip sort");
-    return SM_ERR_VALUE;
-  }
-  if (smem > 48 * 1024)
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-  k_sort_truncate<<<1, 1024, smem, st>>>(nrm, k, strat, perm, s_sorted, errors, ctl, res);
-  note_launch();
-  SM_CUDA_CHECK(cudaGetLastError());
+  SM_CHECK(sort_truncate(st, nrm, k, strat, perm, s_sorted, errors, ctl, res));
   SplitResult* h = reinterpret_cast<SplitResult*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(h, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -1157,92 +1208,91 @@ __global__ void k_ns_matrix(const T* __restrict__ M, int k, T* __restrict__ F) {
   }
 }
 
-// out[j] = |C[:, j]| for C (rows x cols, row-major)
+// Final step of a mixed split, one CTA of 1024 threads, on G = C^H C of the
+// refined rows (C = W V^H, kw x cnt):
+//  * s_j = |C[:, j]| = sqrt(G_jj), sorted descending (perm) and truncated by
+//    the strategy's rule (status and sweeps from the cluster's ctl);
+//  * relative-norm-squared rule (exact_rule): D = the smallest rank whose
+//    discarded weight |A|^2 - sum_{j<D} s_j^2 is at most tol |A|^2, clamped to
+//    max_bond_dimension.  The weights are exact: s_j^2 are Rayleigh quotients
+//    of orthonormal rows and |A|^2 (info[0]) was summed in FP64 from A itself
+//    (cython/truncation.pxi:251-287 states the same contract through the
+//    sorted singular values);
+//  * mixed_info (err2, info[2], info[3], info[7]);
+//  * coupling check, info[4]: the largest state change left by the coupling
+//    between a kept row i and a dropped row j, angle |G_ij| / (lambda_i -
+//    lambda_j) (lambda = s^2) times s_i / |A|_F; its square bounds the
+//    fidelity error the split can add.  Pairs whose both values lie below the
+//    FP32 resolution (s < blind s_0) are skipped: which of two unresolved
+//    directions is kept does not matter once the kept weight is exact.
+// Dynamic shared memory: 24 cnt + 8 bytes.
 template <typename T>
-__global__ void k_col_norms(const T* __restrict__ C, int rows, int cols, double* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= cols) return;
-  double a = 0.0;
-  for (int i = 0; i < rows; ++i) a += S<T>::abs2(C[(size_t)i * cols + j]);
-  out[j] = sqrt(a);
-}
-
-// Exact discarded weight |A|^2 - sum_{j<D} s_j^2 into the split result.
-// Relative-norm-squared rule on exact weights: D = the smallest rank whose
-// discarded weight |A|^2 - sum_{j<D} s_j^2 (exact: s_j^2 are Rayleigh
-// quotients of orthonormal rows, |A|^2 was summed in FP64 from A itself) is at
-// most tol |A|^2, then clamped to max_bond_dimension (cython/truncation.pxi:
-// 251-287 states the same contract through the sorted singular values).
-// Overrides the rank the sorted-value rule gave; one thread.
-__global__ void k_exact_weight_rank(SplitResult* res, const double* __restrict__ s, int cnt,
-                                    sm_strategy st, const double* info) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const double total = info[0];
-  const double allowed = st.tolerance * total;
-  double kept = 0.0;
-  int D = cnt;
-  for (int j = 0; j < cnt; ++j) {
-    kept += s[j] * s[j];
-    if (total - kept <= allowed) {
-      D = j + 1;
-      break;
+__global__ void __launch_bounds__(1024) k_mixed_final(const T* __restrict__ G, int cnt,
+                                                      sm_strategy st, int exact_rule, double blind,
+                                                      const JacobiCtl* ctl, int* perm,
+                                                      double* s_sorted, double* errors,
+                                                      SplitResult* res, double* info) {
+  extern __shared__ unsigned long long keys[];
+  double* ss = reinterpret_cast<double*>(keys + cnt);
+  double* er = ss + cnt;
+  __shared__ double red[32];
+  __shared__ int Dsh;
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    const double g = fmax(0.0, S<T>::real(G[(size_t)i * cnt + i]));
+    keys[i] = (unsigned long long)__double_as_longlong(sqrt(g));
+  }
+  __syncthreads();
+  rank_sort(keys, cnt, perm, s_sorted, ss);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int D;
+    double e;
+    truncate_rule(ss, cnt, st, er, &D, &e);
+    res->status = ctl->status;
+    res->sweeps = ctl->sweeps;
+    for (int i = 0; i < cnt; ++i)
+      if (!(ss[i] == ss[i]) || ss[i] > DBL_MAX) res->status |= DEV_NONFINITE;
+    if (exact_rule) {
+      const double total = info[0];
+      const double allowed = st.tolerance * total;
+      double kept = 0.0;
+      D = cnt;
+      for (int j = 0; j < cnt; ++j) {
+        kept += ss[j] * ss[j];
+        if (total - kept <= allowed) {
+          D = j + 1;
+          break;
+        }
+      }
+      D = max(1, min(D, st.max_bond_dimension));
     }
+    res->D = D;
+    mixed_info(ss, cnt, D, res, info);
+    Dsh = D;
   }
-  D = max(1, min(D, st.max_bond_dimension));
-  res->D = D;
-}
-
-// Also info[2] = s[0], info[3] = s[D-1] for the host's checks.
-// info[7] = |A|^2 - sum of all cnt values^2: the weight outside the rows'
-// span (what a capped QR left behind).
-__global__ void k_mixed_err(SplitResult* res, const double* __restrict__ s, double* info, int cnt) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double kept_D = 0.0, kept_all = 0.0;
-  for (int j = 0; j < cnt; ++j) {
-    if (j == res->D) kept_D = kept_all;
-    kept_all += s[j] * s[j];
-  }
-  if (res->D >= cnt) kept_D = kept_all;
-  res->err2 = fmax(0.0, info[0] - kept_D);
-  info[2] = s[0];
-  info[3] = s[max(res->D, 1) - 1];
-  info[7] = fmax(0.0, info[0] - kept_all);
-}
-
-// Largest state change left by the coupling between a kept row i and a
-// dropped row j after the refinement: the angle |G_ij| / (lambda_i - lambda_j)
-// (G = C^H C of the final rows, lambda = s^2 in sorted order) moves the
-// truncated matrix by about angle * s_i, so the check takes
-// max angle * s_i / |A|_F; its square bounds the fidelity error the split can
-// add.  Writes info[4].
-// Pairs whose both values lie below the FP32 resolution (s < blind s_0) are
-// skipped: which of two unresolved directions is kept does not matter once
-// the kept weight is exact (the rank comes from the exact discarded weight).
-template <typename T>
-__global__ void k_cut_check(const T* __restrict__ G, int cnt, const int* __restrict__ perm,
-                            const double* __restrict__ s, const SplitResult* res, double blind,
-                            double* info) {
-  __shared__ double red[256];
-  const int D = res->D;
-  const double sb = blind * s[0];
+  __syncthreads();
+  for (int i = threadIdx.x; i <= cnt; i += blockDim.x) errors[i] = er[i];
+  const int D = Dsh;
+  const double sb = blind * ss[0];
   const double rnorm = info[0] > 0.0 ? 1.0 / sqrt(info[0]) : 0.0;
   double worst = 0.0;
   const long pairs = (long)D * (cnt - D);
   for (long e = threadIdx.x; e < pairs; e += blockDim.x) {
     const int a = (int)(e / (cnt - D)), b = D + (int)(e % (cnt - D));
-    if (s[a] < sb && s[b] < sb) continue;
-    const double gap = s[a] * s[a] - s[b] * s[b];
+    if (ss[a] < sb && ss[b] < sb) continue;
+    const double gap = ss[a] * ss[a] - ss[b] * ss[b];
     const double g = sqrt(S<T>::abs2(G[(size_t)perm[a] * cnt + perm[b]]));
     const double th = gap > 0.0 ? g / gap : (g > 0.0 ? 1e300 : 0.0);
-    worst = fmax(worst, th * s[a] * rnorm);
+    worst = fmax(worst, th * ss[a] * rnorm);
   }
-  red[threadIdx.x] = worst;
+  for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = worst;
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
-    __syncthreads();
+  if (threadIdx.x < 32) {
+    double w = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) w = fmax(w, __shfl_xor_sync(0xffffffffu, w, o));
+    if (threadIdx.x == 0) info[4] = w;
   }
-  if (threadIdx.x == 0) info[4] = red[0];
 }
 
 // Factors from the refined rows V (cnt x l) and C = W V^H (kw x cnt).
@@ -1346,15 +1396,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // FP32 singular values: sorted, and the rank the rule gives on them; for the
   // singular-value rules a cut below the FP32 resolution sends the split to
   // the FP64 path right away
-  const size_t sort_smem = sizeof(unsigned long long) * (size_t)kcap;
-  if (sort_smem > 48 * 1024)
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sort_smem));
-  k_sort_truncate<<<1, 1024, sort_smem, st>>>(nrm, kcap, strat, perm, s_sorted, errors, ctl, res);
-  note_launch();
-  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info, kcap);
-  note_launch();
-  SM_CUDA_CHECK(cudaGetLastError());
+  SM_CHECK(sort_truncate(st, nrm, kcap, strat, perm, s_sorted, errors, ctl, res, info));
   Head* h = reinterpret_cast<Head*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(&h->c, ctl, sizeof(JacobiCtl), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaMemcpyAsync(h->info, info, 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1429,19 +1471,13 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(normalise(V));
   // 3. singular values, truncation, exact discarded weight
   SM_CHECK(w_vh(V, Cb));
-  k_col_norms<T><<<(cnt + 127) / 128, 128, 0, st>>>(Cb, kw, cnt, cn);
-  note_launch();
-  const size_t smem2 = sizeof(unsigned long long) * (size_t)cnt;
-  k_sort_truncate<<<1, 1024, smem2, st>>>(cn, cnt, strat, perm, s_sorted, errors, ctl, res);
-  note_launch();
-  if (exact_rule) {
-    k_exact_weight_rank<<<1, 1, 0, st>>>(res, s_sorted, cnt, strat, info);
-    note_launch();
-  }
-  k_mixed_err<<<1, 1, 0, st>>>(res, s_sorted, info, cnt);
-  note_launch();
   SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
-  k_cut_check<T><<<1, 256, 0, st>>>(Gb, cnt, perm, s_sorted, res, kMixedBlind, info);
+  const size_t fin_smem = sizeof(double) * (3 * (size_t)cnt + 1);
+  if (fin_smem > 48 * 1024)
+    SM_CUDA_CHECK(cudaFuncSetAttribute(k_mixed_final<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fin_smem));
+  k_mixed_final<T><<<1, 1024, fin_smem, st>>>(Gb, cnt, strat, exact_rule ? 1 : 0, kMixedBlind, ctl,
+                                              perm, s_sorted, errors, res, info);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   SplitResult* hr = reinterpret_cast<SplitResult*>(ctx.pinned);
@@ -1599,17 +1635,7 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
   k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
-  const size_t smem = sizeof(unsigned long long) * (size_t)k;
-  if (smem > 200 * 1024) {
-    set_error("svd: matrix too large for the on-chip sort");
-    return SM_ERR_VALUE;
-  }
-  if (smem > 48 * 1024)
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-  k_sort_truncate<<<1, 1024, smem, st>>>(nrm, k, strat, perm, s_sorted, errors, ctl, res);
-  note_launch();
-  SM_CUDA_CHECK(cudaGetLastError());
+  SM_CHECK(sort_truncate(st, nrm, k, strat, perm, s_sorted, errors, ctl, res));
   SplitResult* h = reinterpret_cast<SplitResult*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(h, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -1844,10 +1870,7 @@ int left_orth_2site_noalloc(cudaStream_t st, const T* A, int m, int n, const sm_
   k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
-  k_sort_truncate<<<1, 1024, sizeof(unsigned long long) * (size_t)k, st>>>(
-      nrm, k, strat, perm, s_sorted, errors, ctl, res);
-  note_launch();
-  SM_CUDA_CHECK(cudaGetLastError());
+  SM_CHECK(sort_truncate(st, nrm, k, strat, perm, s_sorted, errors, ctl, res));
   SplitResult h;
   SM_CUDA_CHECK(cudaMemcpyAsync(&h, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
