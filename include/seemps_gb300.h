@@ -167,6 +167,16 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
             const void* A, int lda, const void* B, int ldb, void* C, int ldc,
             void* stream);
 
+/* The same product at FP32 accuracy: the contractions of the mixed precision
+ * forms (sm_ctx_set_contraction_bits(ctx, 32)).  Real operands with
+ * M, N >= 64, K >= 32 and at least 4 Mi multiply-adds run 3xTF32 on the
+ * tensor cores (tcgen05, FP32 accumulation); other shapes and complex
+ * operands run an FP32 SIMT kernel.  No reference counterpart (the reference
+ * contracts in FP64). */
+int sm_gemm_f32(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
+                const void* A, int lda, const void* B, int ldb, void* C, int ldc,
+                void* stream);
+
 /* _destructive_svd (cython/svd.pxi:17-83): economy SVD A[m,n] = U diag(s) Vt,
  * s descending; U is m x r, Vt is r x n, r = min(m, n).  A is not modified. */
 int sm_svd(void* ctx, int dtype, const void* A, int m, int n, void* U, double* s,
@@ -310,6 +320,7 @@ typedef struct sm_stats {
   int64_t gemm32_launches;     /* contractions computed in FP32 (mixed forms) */
   double gemm32_flops;
   double gemm32_ms;            /* event-timed (stats timing on) */
+  int64_t gemm_tc_launches;    /* of those, on the tensor cores (3xTF32, tcgen05) */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

@@ -74,6 +74,7 @@ class sm_stats(C.Structure):
         ("gemm32_launches", C.c_int64),
         ("gemm32_flops", C.c_double),
         ("gemm32_ms", C.c_double),
+        ("gemm_tc_launches", C.c_int64),
     ]
 
 
@@ -96,6 +97,8 @@ SIGNATURES = {
     "sm_truncate": (C.c_int, [vp, vp, C.c_int, stp, ip, dp, vp]),
     "sm_gemm": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int,
                           vp, C.c_int, vp, C.c_int, vp]),
+    "sm_gemm_f32": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp,
+                              C.c_int, vp, C.c_int, vp, C.c_int, vp]),
     "sm_svd": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp]),
     "sm_left_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,
                                      vp, ip, dp, vp]),

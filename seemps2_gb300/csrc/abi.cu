@@ -275,6 +275,27 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const v
                         (const cplx*)A, lda, (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc);
 }
 
+int sm_gemm_f32(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const void* A,
+                int lda, const void* B, int ldb, void* C, int ldc, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (opA < 0 || opA > 2 || opB < 0 || opB > 2 || M < 0 || N < 0 || K < 0) {
+    set_error("sm_gemm_f32: invalid op flag or size");
+    return SM_ERR_VALUE;
+  }
+  Ctx& c = *as_ctx(ctx);
+  cudaStream_t s = as_stream(stream);
+  int rc;
+  if (dtype == SM_FLOAT64)
+    rc = gemm_ctx_f32<double>(c, s, opA, opB, M, N, K, 1.0, (const double*)A, lda,
+                              (const double*)B, ldb, 0.0, (double*)C, ldc);
+  else
+    rc = gemm_ctx_f32<cplx>(c, s, opA, opB, M, N, K, cplx{1.0, 0.0}, (const cplx*)A, lda,
+                            (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc);
+  SM_CHECK(rc);
+  return tc_status_check(c, s);
+}
+
 int sm_svd(void* ctx, int dtype, const void* A, int m, int n, void* U, double* s, void* Vt,
            void* stream) {
   SM_GUARD_CTX(ctx);

@@ -334,6 +334,21 @@ int gemm_ctx_f32(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int 
   if (M == 0 || N == 0 || K == 0) return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   ctx.stats.gemm32_launches += 1;
   ctx.stats.gemm32_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (gemm_tc_eligible(M, N, K)) {
+      if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+      SM_CHECK(gemm_tc(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc));
+      ctx.stats.gemm_tc_launches += 1;
+      if (ctx.timing) {
+        SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+        SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
+        float ms = 0.f;
+        SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+        ctx.stats.gemm32_ms += ms;
+      }
+      return SM_OK;
+    }
+  }
   // FP32 runs 64x the FP64 rate: split K only when the output has very few tiles
   const int nz = splitk_slices(M, N, K, std::max(1, ctx.num_sms) / 2);
   T* part = nullptr;

@@ -1,0 +1,432 @@
+// Tensor-core GEMM for FP64 operands at FP32 accuracy: 3xTF32 on tcgen05.
+//
+//   C[M,N] = alpha * op(A)[M,K] * op(B)[K,N] + beta * C      (real, row-major)
+//
+// The mixed precision forms run the sweep contractions (cython/gemm.pxi:21-122
+// in the reference, FP64 there) at FP32 accuracy.  GB300's CUDA cores give
+// FP32 at 64x the FP64 rate, its tensor cores TF32 at another ~15x; TF32 keeps
+// 11 significant bits, so each operand is split x = hi + lo (hi = x rounded to
+// TF32, lo = the FP32 rest) and the product is hi*hi + hi*lo + lo*hi
+// accumulated in FP32 in tensor memory: the error of an FP32 GEMM.
+//
+// Data path per 128 x 128 output tile (one CTA of 128 threads, K split over
+// blockIdx.z when the output has few tiles):
+//   * a split kernel writes hi / lo of op(A) as M x Kp and of op(B)^T as
+//     N x Kp FP32 arrays (K contiguous, Kp = K rounded up to 32, zero pad);
+//   * warp 0 / lane 0 streams 32-wide K slices of the four arrays with TMA
+//     (cp.async.bulk.tensor, 128-byte swizzle) into a 3-stage ring;
+//   * warp 1 / lane 0 issues tcgen05.mma kind::tf32 (M=128, N=128, K=8; three
+//     per K step) accumulating in 128 TMEM columns, and tcgen05.commit frees
+//     each stage;
+//   * all four warps read the accumulator back with tcgen05.ld (warp w owns
+//     TMEM lanes 32w..32w+31 = tile rows) and write FP64 results.
+// Every mbarrier wait is bounded (globaltimer): on timeout the CTA records an
+// error bit, waits (bounded) for its own copies in flight, frees its TMEM and
+// returns; the sweep reads the status word at its end.
+#include <algorithm>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "kernels.cuh"
+
+namespace sm {
+
+namespace {
+
+constexpr int TM = 128, TN = 128, TK = 32, TS = 3;
+constexpr int kTCThreads = 128;
+constexpr uint32_t kTileA = TM * TK * 4;  // bytes of one 128 x 32 FP32 slice
+constexpr uint32_t kTileB = TN * TK * 4;
+constexpr uint32_t kStage = 2 * kTileA + 2 * kTileB;
+constexpr size_t kTCSmem = (size_t)TS * kStage + 1024 + 256;
+// instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9 and
+// 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                            ((uint32_t)(TM >> 4) << 24);
+constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s per wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase of the given parity; false after `ns` nanoseconds.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, unsigned long long ns) {
+  if (mbar_try_wait(b, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try_wait(b, parity))
+    if (gtimer() - t0 > ns) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x,
+                                            int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+      "%4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// K-major operand in the 128-byte swizzled layout TMA writes: rows of 128 B,
+// 8-row atoms of 1024 B (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;              // leading byte offset (unused for this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;              // descriptor version
+  d |= (uint64_t)2 << 61;              // 128-byte swizzle
+  return d;
+}
+__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(kTCThreads, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+              const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
+              int M, int N, int ktiles, int kt_per, double alpha, double beta,
+              double* __restrict__ C, int ldc, double* __restrict__ part,
+              unsigned int* __restrict__ status) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)TS * kStage);
+  uint64_t* empty = full + TS;
+  uint64_t* done = empty + TS;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+  const int kt0 = blockIdx.z * kt_per;
+  const int nk = min(ktiles, kt0 + kt_per) - kt0;  // >= 1 (host)
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"((uint32_t)TN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // producer: TMA ring
+    int issued[TS] = {};
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % TS;
+      const uint32_t ph = (uint32_t)(i / TS) & 1u;
+      if (i >= TS && !mbar_wait(&empty[s], ph ^ 1u, kWaitNs)) {
+        atomicOr(status, 1u);
+        break;
+      }
+      unsigned char* stg = base + (size_t)s * kStage;
+      mbar_expect_tx(&full[s], kStage);
+      const int x = (kt0 + i) * TK;
+      tma_load_2d(stg, &mAh, &full[s], x, m0);
+      tma_load_2d(stg + kTileA, &mAl, &full[s], x, m0);
+      tma_load_2d(stg + 2 * kTileA, &mBh, &full[s], x, n0);
+      tma_load_2d(stg + 2 * kTileA + kTileB, &mBl, &full[s], x, n0);
+      issued[s] += 1;
+    }
+    // no copy of this CTA may still be landing when it exits
+    for (int s = 0; s < TS; ++s)
+      if (issued[s] && !mbar_wait(&full[s], (uint32_t)(issued[s] - 1) & 1u, kWaitNs))
+        atomicOr(status, 4u);
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % TS;
+      const uint32_t ph = (uint32_t)(i / TS) & 1u;
+      if (!mbar_wait(&full[s], ph, kWaitNs)) {
+        atomicOr(status, 2u);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t ah = smem_u32(base + (size_t)s * kStage);
+      const uint32_t al = ah + kTileA, bh = ah + 2 * kTileA, bl = bh + kTileB;
+#pragma unroll
+      for (int kk = 0; kk < TK / 8; ++kk) {
+        const uint32_t off = kk * 32;  // 8 TF32 values
+        const uint64_t dah = sdesc_sw128(ah + off), dal = sdesc_sw128(al + off);
+        const uint64_t dbh = sdesc_sw128(bh + off), dbl = sdesc_sw128(bl + off);
+        umma_tf32(tmem, dah, dbh, (i > 0 || kk > 0) ? 1u : 0u);
+        umma_tf32(tmem, dah, dbl, 1u);
+        umma_tf32(tmem, dal, dbh, 1u);
+      }
+      umma_commit(&empty[s]);
+    }
+    umma_commit(done);  // arrives once every MMA issued above has completed
+  }
+  __syncwarp();
+  // epilogue: the done wait outlasts the producer's and the issuer's bounds
+  const bool ok = mbar_wait(done, 0u, 4 * kWaitNs);
+  __syncwarp();
+  tc_fence_after();
+  if (ok) {
+    const int row = m0 + warp * 32 + lane;
+    for (int c = 0; c < TN; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = n0 + c + j;
+          if (col < N) {
+            if (part) {
+              part[((size_t)blockIdx.z * M + row) * N + col] = (double)v[j];
+            } else {
+              double* p = C + (size_t)row * ldc + col;
+              *p = beta == 0.0 ? alpha * (double)v[j] : fma(alpha, (double)v[j], beta * *p);
+            }
+          }
+        }
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    atomicOr(status, 8u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((uint32_t)TN)
+                 : "memory");
+  }
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// hi / lo FP32 parts of op(X) as a rows x kp K-contiguous array: element
+// (r, k) is X[r * ldx + k] (trans = 0) or X[k * ldx + r] (trans = 1), zero for
+// k >= K.  32 x 32 tiles through shared memory so both sides stay coalesced.
+__global__ void k_split_tf32(const double* __restrict__ X, int ldx, int rows, int K, int kp,
+                             int trans, float* __restrict__ hi, float* __restrict__ lo) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int j = ty; j < 32; j += 8) {
+    double v = 0.0;
+    if (trans) {  // read along r: tile[k][r]
+      const int k = k0 + j, r = r0 + tx;
+      if (k < K && r < rows) v = X[(size_t)k * ldx + r];
+      tile[j][tx] = v;
+    } else {  // read along k: tile[r][k]
+      const int r = r0 + j, k = k0 + tx;
+      if (k < K && r < rows) v = X[(size_t)r * ldx + k];
+      tile[j][tx] = v;
+    }
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int r = r0 + j, k = k0 + tx;
+    if (r < rows && k < kp) {
+      const double v = trans ? tile[tx][j] : tile[j][tx];
+      const float h = tf32_rna((float)v);
+      hi[(size_t)r * kp + k] = h;
+      lo[(size_t)r * kp + k] = (float)(v - (double)h);
+    }
+  }
+}
+
+__global__ void k_tc_reduce(int M, int N, int nz, const double* __restrict__ part, double alpha,
+                            double beta, double* __restrict__ C, int ldc) {
+  const size_t mn = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < mn;
+       e += (size_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int z = 0; z < nz; ++z) acc += part[(size_t)z * mn + e];
+    double* p = C + (e / N) * ldc + (e % N);
+    *p = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *p);
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+int make_map(CUtensorMap* map, const float* base, int rows, int kp, int box_rows) {
+  auto enc = encode_fn();
+  if (!enc) {
+    set_error("tensor-core GEMM: cuTensorMapEncodeTiled not available");
+    return SM_ERR_CUDA;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kp * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims,
+                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("tensor-core GEMM: tensor map encoding failed");
+    return SM_ERR_CUDA;
+  }
+  return SM_OK;
+}
+
+}  // namespace
+
+bool gemm_tc_eligible(int M, int N, int K) {
+  // below a few tiles of work the SIMT FP32 kernel is as fast and has no
+  // split step
+  return (double)M * N * K >= 4.0 * 1024 * 1024 && M >= 64 && N >= 64 && K >= 32 &&
+         encode_fn() != nullptr;
+}
+
+int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
+            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc) {
+  const int kp = (K + TK - 1) / TK * TK;
+  const int ktiles = kp / TK;
+  float *ah, *al, *bh, *bl;
+  unsigned int* status;
+  SM_CHECK(ctx.scratch("tc.Ah", (size_t)M * kp, &ah));
+  SM_CHECK(ctx.scratch("tc.Al", (size_t)M * kp, &al));
+  SM_CHECK(ctx.scratch("tc.Bh", (size_t)N * kp, &bh));
+  SM_CHECK(ctx.scratch("tc.Bl", (size_t)N * kp, &bl));
+  SM_CHECK(tc_status(ctx, &status));
+  // op(A)[m][k]: A[m][k] (N) or A[k][m] (T, C: real); op(B)^T[n][k]: B[k][n]
+  // (N) or B[n][k] (T, C)
+  const dim3 sblk(32, 8);
+  k_split_tf32<<<dim3(kp / 32, (M + 31) / 32), sblk, 0, st>>>(A, lda, M, K, kp,
+                                                              opA == SM_OP_N ? 0 : 1, ah, al);
+  note_launch();
+  k_split_tf32<<<dim3(kp / 32, (N + 31) / 32), sblk, 0, st>>>(B, ldb, N, K, kp,
+                                                              opB == SM_OP_N ? 1 : 0, bh, bl);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  CUtensorMap mAh, mAl, mBh, mBl;
+  SM_CHECK(make_map(&mAh, ah, M, kp, TM));
+  SM_CHECK(make_map(&mAl, al, M, kp, TM));
+  SM_CHECK(make_map(&mBh, bh, N, kp, TN));
+  SM_CHECK(make_map(&mBl, bl, N, kp, TN));
+  const int tiles = ((M + TM - 1) / TM) * ((N + TN - 1) / TN);
+  int nz = std::max(1, std::min(std::max(1, ctx.num_sms) / tiles, ktiles / 2));
+  const int kt_per = (ktiles + nz - 1) / nz;
+  nz = (ktiles + kt_per - 1) / kt_per;
+  double* part = nullptr;
+  if (nz > 1) SM_CHECK(ctx.scratch("tc.part", (size_t)nz * M * N, &part));
+  static bool attr = false;
+  if (!attr) {
+    SM_CUDA_CHECK(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kTCSmem));
+    attr = true;
+  }
+  const dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, nz);
+  k_gemm_tc<<<grid, kTCThreads, kTCSmem, st>>>(mAh, mAl, mBh, mBl, M, N, ktiles, kt_per, alpha,
+                                               beta, C, ldc, part, status);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  if (nz > 1) {
+    const size_t mn = (size_t)M * N;
+    k_tc_reduce<<<(int)std::min<size_t>((mn + 255) / 256, 4096), 256, 0, st>>>(M, N, nz, part,
+                                                                               alpha, beta, C, ldc);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+  }
+  return SM_OK;
+}
+
+int tc_status(Ctx& ctx, unsigned int** out) {
+  auto it = ctx.bufs.find("tc.status");
+  const bool fresh = it == ctx.bufs.end();
+  SM_CHECK(ctx.scratch("tc.status", sizeof(unsigned int), reinterpret_cast<void**>(out)));
+  if (fresh) SM_CUDA_CHECK(cudaMemset(*out, 0, sizeof(unsigned int)));
+  return SM_OK;
+}
+
+int tc_status_check(Ctx& ctx, cudaStream_t st) {
+  if (ctx.bufs.find("tc.status") == ctx.bufs.end()) return SM_OK;
+  unsigned int* status;
+  SM_CHECK(tc_status(ctx, &status));
+  unsigned int* h = reinterpret_cast<unsigned int*>(ctx.pinned) + 1000;
+  SM_CUDA_CHECK(cudaMemcpyAsync(h, status, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  if (*h) {
+    SM_CUDA_CHECK(cudaMemsetAsync(status, 0, sizeof(unsigned int), st));
+    set_error("tensor-core GEMM: a pipeline wait timed out (status " + std::to_string(*h) + ")");
+    return SM_ERR_CUDA;
+  }
+  return SM_OK;
+}
+
+}  // namespace sm

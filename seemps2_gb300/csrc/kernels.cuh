@@ -105,6 +105,17 @@ template <typename T>
 int gemm_ctx_f32(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha,
                  const T* A, int lda, const T* B, int ldb, T beta, T* C, int ldc);
 
+// --- gemm_tc.cu -------------------------------------------------------------
+// Real GEMM at FP32 accuracy on the tensor cores (3xTF32, tcgen05): used by
+// gemm_ctx_f32 for shapes gemm_tc_eligible accepts.  Pipeline waits that time
+// out set bits of a device status word; tc_status_check reads (and clears) it
+// and returns SM_ERR_CUDA when one did.
+bool gemm_tc_eligible(int M, int N, int K);
+int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
+            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc);
+int tc_status(Ctx& ctx, unsigned int** out);
+int tc_status_check(Ctx& ctx, cudaStream_t st);
+
 // --- mps_ops.cu ------------------------------------------------------------
 template <typename T>
 int scale_matrix(cudaStream_t st, int M, int N, T beta, T* C, int ldc);

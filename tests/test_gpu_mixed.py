@@ -272,6 +272,7 @@ def test_mixed_fp32_contractions_apply():
         sg.set_precision("fp64")
     res = so.mpo_apply(mpo, mps, so.DEFAULT_STRATEGY.replace(**kw))
     assert stats["gemm32_launches"] > 50
+    assert stats["gemm_tc_launches"] > 0  # the larger contractions run on the tensor cores
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-10, fe
     assert abs(out.error() - res.error) <= 1e-4 * res.error + 1e-12, (out.error(), res.error)

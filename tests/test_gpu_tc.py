@@ -1,0 +1,90 @@
+"""Tensor-core GEMM at FP32 accuracy (3xTF32 on tcgen05, sm_gemm_f32) against
+an FP64 product: relative Frobenius error below 2e-6 for every op pair,
+ragged sizes (M, N not multiples of the 128 x 128 tile, K not a multiple of
+the 32-wide slice) and split-K; small shapes go to the FP32 SIMT kernel
+instead (no tensor-core launch).  The two-term simplify checks the
+accumulating (beta = 1) contractions of a sum under FP32 contractions."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import seemps_oracle as so
+from tests.gpu_util import mps_np
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import seemps2_gb300 as sg  # noqa: E402
+from seemps2_gb300 import _lib  # noqa: E402
+
+OPS = {"N": 0, "T": 1, "C": 2}
+
+
+def _gemm_f32(opA, opB, A, B, M, N, K):
+    Ad = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    Bd = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    Cd = torch.empty((M, N), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.load().sm_gemm_f32(
+        _lib.context(), _lib.SM_FLOAT64, OPS[opA], OPS[opB], M, N, K, C.c_void_p(Ad.data_ptr()),
+        A.shape[1], C.c_void_p(Bd.data_ptr()), B.shape[1], C.c_void_p(Cd.data_ptr()), N,
+        _lib.stream_handle()))
+    torch.cuda.synchronize()
+    return Cd.cpu().numpy()
+
+
+@pytest.mark.parametrize("M,N,K,opA,opB", [
+    (128, 128, 256, "N", "N"),
+    (256, 1536, 768, "N", "N"),   # left environment x product site (chi 256, D 3)
+    (1536, 256, 768, "N", "T"),
+    (512, 512, 768, "C", "N"),
+    (300, 200, 100, "T", "T"),    # ragged in all three
+    (64, 64, 1024, "N", "C"),     # one tile, deep K: split-K
+    (1000, 130, 40, "T", "N"),
+])
+def test_tensor_core_gemm_matches_fp64(M, N, K, opA, opB):
+    rng = np.random.default_rng(M + 7 * N + 13 * K)
+    A = rng.normal(size=(M, K) if opA == "N" else (K, M))
+    B = rng.normal(size=(K, N) if opB == "N" else (N, K))
+    ref = (A if opA == "N" else A.T) @ (B if opB == "N" else B.T)
+    _lib.stats_reset()
+    out = _gemm_f32(opA, opB, A, B, M, N, K)
+    st = _lib.stats_read()
+    assert st["gemm_tc_launches"] == 1
+    rel = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    assert rel < 2e-6, rel
+    # better than a plain FP32 product of the rounded operands would allow by far
+    assert np.isfinite(out).all()
+
+
+def test_small_shapes_stay_on_simt():
+    rng = np.random.default_rng(3)
+    A = rng.normal(size=(40, 30))
+    B = rng.normal(size=(30, 20))
+    _lib.stats_reset()
+    out = _gemm_f32("N", "N", A, B, 40, 20, 30)
+    assert _lib.stats_read()["gemm_tc_launches"] == 0
+    assert np.linalg.norm(out - A @ B) / np.linalg.norm(A @ B) < 1e-6
+
+
+def test_fp32_contractions_of_a_sum():
+    rng = np.random.default_rng(8)
+    n, chi = 18, 128
+    states = [so.random_mps(2, n, chi, rng) for _ in range(2)]
+    kw = dict(tolerance=1e-12, max_bond_dimension=chi, max_sweeps=2, simplification_tolerance=0.0)
+    st = sg.DEFAULT_STRATEGY.replace(**kw)
+    sg.set_precision("mixed", contractions="fp32")
+    _lib.stats_reset()
+    try:
+        out = sg.simplify(sg.MPSSum([0.6, -0.4], [sg.MPS(s) for s in states]), strategy=st)
+        stats = _lib.stats_read()
+    finally:
+        sg.set_precision("fp64")
+    res = so.simplify_mps_sum([0.6, -0.4], states, so.DEFAULT_STRATEGY.replace(**kw))
+    assert stats["gemm_tc_launches"] > 10, stats["gemm_tc_launches"]
+    fe = so.fidelity_error(mps_np(out), res.tensors)
+    assert fe < 1e-10, fe
