@@ -12,9 +12,10 @@ Reported (one JSON line on rank 0):
   value        sweeps/s with inputs resident in GPU memory (CUDA events)
   e2e          same through the public API from pinned host arrays, host<->device
                copies inside the timed region
-  roofline     the dominant kernel (the FP64 Jacobi SVD): algorithmic flops per
-               launch / event-timed launch duration vs the FP64 peak measured in
-               this run (the library's FP64 GEMM; GB300 has no FP64 tensor path)
+  roofline     the dominant FP64 kernel (FP64 GEMM or Jacobi SVD): algorithmic
+               flops per launch / event-timed launch duration vs the FP64 peak
+               measured in this run (the library's FP64 GEMM; GB300 has no FP64
+               tensor path); plus the tensor-core GEMM of the FP32 contractions
   cpu_baseline the CPU oracle (NumPy/SciPy LAPACK, all host threads) on the
                same workload
 `--impl reference` times that CPU implementation alone, same workload.
@@ -126,6 +127,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def measured_bf16_tflops() -> float:
+    """Dense BF16 TFLOP/s measured on the GB300s (MEASURED_PEAKS.json, burst
+    figure); 1900 (an earlier GB300 measurement) when the file is absent."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        return 1900.0
+
+
 def fp64_peak(torch, lib_mod) -> float:
     """Measured FP64 FLOP/s of this GPU: best of the library's FP64 GEMM (2048^3)."""
     import ctypes as C
@@ -200,7 +211,7 @@ def workload_config(args):
                         f"+ variational simplify, tol 1e-12, max bond {args.chi}, 2 sweeps",
             "n": args.n, "chi": args.chi, "mpo_bond": 3, "tolerance": 1e-12,
             "max_bond_dimension": args.chi, "sweeps_per_step": 2, "form": args.form,
-            "contractions": getattr(args, "contractions", "fp64"),
+            "contractions": getattr(args, "contractions", "fp32"),
             "l2": "flushed between timed steps (256 MB write); the product MPS is >256 MB",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
@@ -252,6 +263,55 @@ def run_split_case(args):
     print(json.dumps(out), flush=True)
 
 
+def run_gemm_case(args):
+    """One real M x N x K product (op N, N) timed with CUDA events: the FP64 SIMT
+    GEMM, the tensor-core 3xTF32 GEMM (FP32 accuracy) and the FP64-accurate
+    tensor-core GEMM (BF16 slices), each with its operand preparation and
+    split-K reduction."""
+    import ctypes as C
+
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from seemps2_gb300 import _lib
+
+    M, N, K = args.gemm_case
+    rng = np.random.default_rng(SEED)
+    A = torch.from_numpy(rng.normal(size=(M, K))).cuda()
+    B = torch.from_numpy(rng.normal(size=(K, N))).cuda()
+    out = {"gemm_case": [M, N, K], "steps": args.steps}
+    ref = None
+    for name, fn in (("fp64", "sm_gemm"), ("tf32x3", "sm_gemm_f32"),
+                     ("fp64_tensor_cores", "sm_gemm_f64tc")):
+        Cm = torch.empty((M, N), dtype=torch.float64, device="cuda")
+        f = getattr(_lib.load(), fn)
+        call = lambda: _lib.check(f(_lib.context(), 0, 0, 0, M, N, K, C.c_void_p(A.data_ptr()), K,
+                                    C.c_void_p(B.data_ptr()), N, C.c_void_p(Cm.data_ptr()), N,
+                                    _lib.stream_handle()))
+        for _ in range(max(1, args.warmup)):
+            call()
+        torch.cuda.synchronize()
+        _lib.stats_reset()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            call()
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res = Cm.cpu().numpy()
+        if ref is None:
+            ref = res
+        out[name] = {"ms": ms, "tflops": 2.0 * M * N * K / (ms / 1e3) / 1e12,
+                     "tc_launches": _lib.stats_read()["gemm_tc_launches"] / args.steps,
+                     "oz_launches": _lib.stats_read()["gemm_oz_launches"] / args.steps,
+                     "rel_err_vs_fp64": float(np.linalg.norm(res - ref) / np.linalg.norm(ref))}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -264,8 +324,10 @@ def main():
                     help="plain = FP64 splits (reference ranks); mixed = FP32 cluster "
                          "factorisation + FP64 refinement; mixed+learned = mixed with the rank "
                          "predictor capping the FP32 QR (the metric's headline form)")
-    ap.add_argument("--contractions", default="fp64", choices=["fp64", "fp32"],
-                    help="arithmetic of the sweep contractions in the mixed forms")
+    ap.add_argument("--contractions", default="fp32", choices=["fp64", "fp32"],
+                    help="accuracy of the sweep contractions in the mixed forms: fp32 = 3xTF32 "
+                         "on the tensor cores (FP32 SIMT for small or complex shapes); the "
+                         "state norm, the refinement and the final estimate stay FP64")
     ap.add_argument("--rank-model", default=None,
                     help="trained rank predictor (.npz); trained here when absent")
     ap.add_argument("--train-count", type=int, default=90,
@@ -273,9 +335,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--split-case", type=int, nargs=2, metavar=("M", "N"),
                     help="time single M x N two-site splits in both precision modes and exit")
+    ap.add_argument("--gemm-case", type=int, nargs=3, metavar=("M", "N", "K"),
+                    help="time one real M x N x K product on the tensor cores (3xTF32) and as "
+                         "the FP64 GEMM, and exit")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="after the warm-up, run one step of --form between cudaProfilerStart "
+                         "and cudaProfilerStop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()
     if args.split_case:
         return run_split_case(args)
+    if args.gemm_case:
+        return run_gemm_case(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -323,6 +393,21 @@ def main():
 
     # ---- plain FP64 form on the same workload (the metric's comparison) -------
     plain = None
+    if args.profile_step:
+        sg.set_precision({"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed+learned"}[
+            args.form], contractions=args.contractions)
+        for _ in range(max(3, args.warmup)):
+            step()
+        torch.cuda.synchronize()
+        _lib.stats_reset(timing=False)
+        torch.cuda.profiler.start()
+        step()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        stt = _lib.stats_read()
+        print(json.dumps({"profile_step": args.form, "contractions": args.contractions,
+                          "launches": stt["launches"]}), flush=True)
+        return
     if args.form != "plain":
         sg.set_precision("fp64")
         step()
@@ -426,6 +511,30 @@ def main():
         "cluster_share_of_step": stt["cluster_ms"] / inst_ms if inst_ms else None,
         "cluster_bound": "latency (FP32 rotations on 16 SMs, one cluster barrier per block round)",
     }
+    if stt["gemm_oz_launches"]:
+        oz_ach = stt["gemm_oz_flops"] / (stt["gemm_oz_ms"] / 1e3) if stt["gemm_oz_ms"] else 0.0
+        roofline["fp64_tensor_core_gemm"] = {
+            "kernel": "k_gemm_oz (FP64-accurate: 8 BF16 slices, 36 tcgen05 products; slicing "
+                      "and split-K reduce included)",
+            "launches_per_step": stt["gemm_oz_launches"],
+            "flops_per_launch": stt["gemm_oz_flops"] / stt["gemm_oz_launches"],
+            "achieved": oz_ach / 1e12, "unit": "TFLOP/s (FP64-equivalent 2MNK / time)",
+            "vs_fp64_peak": oz_ach / peak if peak else None,
+            "share_of_step": stt["gemm_oz_ms"] / inst_ms if inst_ms else None,
+        }
+    if stt["gemm_tc_launches"]:
+        tc_ach = stt["gemm_tc_flops"] / (stt["gemm_tc_ms"] / 1e3) if stt["gemm_tc_ms"] else 0.0
+        tf32_peak = measured_bf16_tflops() / 2.0
+        roofline["tensor_core_gemm"] = {
+            "kernel": "k_gemm_tc (3xTF32, tcgen05 + TMA; split and split-K reduce included)",
+            "launches_per_step": stt["gemm_tc_launches"],
+            "flops_per_launch": stt["gemm_tc_flops"] / stt["gemm_tc_launches"],
+            "achieved": tc_ach / 1e12, "unit": "TFLOP/s (2MNK / time)",
+            "peak": tf32_peak, "frac": tc_ach / 1e12 / tf32_peak if tf32_peak else None,
+            "peak_source": "half the measured bf16 dense rate (MEASURED_PEAKS.json): GB300 runs "
+                           "TF32 at half the BF16 rate; each product issues 3 TF32 MMAs",
+            "share_of_step": stt["gemm_tc_ms"] / inst_ms if inst_ms else None,
+        }
 
     # ---- CPU baseline (oracle, bounded sample) -------------------------------
     cpu = None

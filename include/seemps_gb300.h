@@ -167,6 +167,23 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
             const void* A, int lda, const void* B, int ldb, void* C, int ldc,
             void* stream);
 
+/* The same product at FP64 accuracy on the BF16 tensor cores (no reference
+ * counterpart): real operands with M, N >= 32, K >= 32 and at least 2 Mi
+ * multiply-adds are scaled by powers of two per row of op(A) / column of
+ * op(B), cut into 8 slices of 7-bit integers (exact in BF16) and multiplied
+ * slice by slice with tcgen05 (Ozaki, Ogita, Oishi and Rump, Numer. Algorithms
+ * 59, 2012), exact FP32 accumulation over chunks of 256 and FP64 across
+ * chunks; the error is that of an FP64 GEMM.  Other shapes and complex
+ * operands run the FP64 SIMT kernel.  The mixed precision forms route their
+ * FP64 products here (sm_ctx_set_fp64_products). */
+int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
+                  const void* A, int lda, const void* B, int ldb, void* C, int ldc,
+                  void* stream);
+/* FP64 products of the mixed forms (state norm, refinement, final estimate,
+ * FP64 contractions): 1 (default) on the tensor cores as sm_gemm_f64tc, 0 on
+ * the FP64 SIMT kernel.  SM_PRECISION_FP64 always uses the SIMT kernel. */
+int sm_ctx_set_fp64_products(void* ctx, int tensor_cores);
+
 /* The same product at FP32 accuracy: the contractions of the mixed precision
  * forms (sm_ctx_set_contraction_bits(ctx, 32)).  Real operands with
  * M, N >= 64, K >= 32 and at least 4 Mi multiply-adds run 3xTF32 on the
@@ -321,6 +338,11 @@ typedef struct sm_stats {
   double gemm32_flops;
   double gemm32_ms;            /* event-timed (stats timing on) */
   int64_t gemm_tc_launches;    /* of those, on the tensor cores (3xTF32, tcgen05) */
+  double gemm_tc_flops;        /* 2 M N K of those (the MMAs run 3x this) */
+  double gemm_tc_ms;           /* event-timed (stats timing on), split + MMA + reduce */
+  int64_t gemm_oz_launches;    /* FP64 products on the BF16 tensor cores (mixed forms) */
+  double gemm_oz_flops;        /* 2 M N K of those */
+  double gemm_oz_ms;           /* event-timed (stats timing on), slicing + MMA + reduce */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

@@ -75,6 +75,11 @@ class sm_stats(C.Structure):
         ("gemm32_flops", C.c_double),
         ("gemm32_ms", C.c_double),
         ("gemm_tc_launches", C.c_int64),
+        ("gemm_tc_flops", C.c_double),
+        ("gemm_tc_ms", C.c_double),
+        ("gemm_oz_launches", C.c_int64),
+        ("gemm_oz_flops", C.c_double),
+        ("gemm_oz_ms", C.c_double),
     ]
 
 
@@ -99,6 +104,9 @@ SIGNATURES = {
                           vp, C.c_int, vp, C.c_int, vp]),
     "sm_gemm_f32": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp,
                               C.c_int, vp, C.c_int, vp, C.c_int, vp]),
+    "sm_gemm_f64tc": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp,
+                                C.c_int, vp, C.c_int, vp, C.c_int, vp]),
+    "sm_ctx_set_fp64_products": (C.c_int, [vp, C.c_int]),
     "sm_svd": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp]),
     "sm_left_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,
                                      vp, ip, dp, vp]),

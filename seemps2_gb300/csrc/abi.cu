@@ -267,12 +267,41 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const v
     set_error("sm_gemm: invalid op flag");
     return SM_ERR_VALUE;
   }
-  // through the context: split-K for small outputs, counted in the stats
+  // through the context (split-K for small outputs, counted in the stats), on
+  // the FP64 SIMT kernel in every precision mode
   if (dtype == SM_FLOAT64)
-    return gemm_ctx<double>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K, 1.0,
-                            (const double*)A, lda, (const double*)B, ldb, 0.0, (double*)C, ldc);
-  return gemm_ctx<cplx>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K, cplx{1.0, 0.0},
-                        (const cplx*)A, lda, (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc);
+    return gemm_ctx_sel<double>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K, 1.0,
+                                (const double*)A, lda, (const double*)B, ldb, 0.0, (double*)C, ldc,
+                                false);
+  return gemm_ctx_sel<cplx>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K, cplx{1.0, 0.0},
+                            (const cplx*)A, lda, (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc,
+                            false);
+}
+
+int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const void* A,
+                  int lda, const void* B, int ldb, void* C, int ldc, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (opA < 0 || opA > 2 || opB < 0 || opB > 2 || M < 0 || N < 0 || K < 0) {
+    set_error("sm_gemm_f64tc: invalid op flag or size");
+    return SM_ERR_VALUE;
+  }
+  Ctx& c = *as_ctx(ctx);
+  cudaStream_t s = as_stream(stream);
+  if (dtype == SM_FLOAT64 && M && N && K && gemm_oz_eligible(M, N, K)) {
+    c.stats.gemm_oz_launches += 1;
+    c.stats.gemm_oz_flops += 2.0 * M * N * K;
+    SM_CHECK(gemm_oz(c, s, opA, opB, M, N, K, 1.0, (const double*)A, lda, (const double*)B, ldb,
+                     0.0, (double*)C, ldc));
+    return tc_status_check(c, s);
+  }
+  return sm_gemm(ctx, dtype, opA, opB, M, N, K, A, lda, B, ldb, C, ldc, stream);
+}
+
+int sm_ctx_set_fp64_products(void* ctx, int tensor_cores) {
+  SM_GUARD_CTX(ctx);
+  as_ctx(ctx)->fp64_tc = tensor_cores != 0;
+  return SM_OK;
 }
 
 int sm_gemm_f32(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const void* A,

@@ -306,7 +306,31 @@ int splitk_slices(int M, int N, int K, int sms) {
 template <typename T>
 int gemm_ctx(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A,
              int lda, const T* B, int ldb, T beta, T* C, int ldc) {
+  return gemm_ctx_sel(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, true);
+}
+
+template <typename T>
+int gemm_ctx_sel(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha,
+                 const T* A, int lda, const T* B, int ldb, T beta, T* C, int ldc, bool allow_tc) {
   if (M == 0 || N == 0 || K == 0) return gemm<T>(st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  if constexpr (sizeof(T) == sizeof(double)) {
+    // mixed forms: FP64-accurate products on the BF16 tensor cores
+    if (allow_tc && ctx.precision != SM_PRECISION_FP64 && ctx.fp64_tc &&
+        gemm_oz_eligible(M, N, K)) {
+      ctx.stats.gemm_oz_launches += 1;
+      ctx.stats.gemm_oz_flops += 2.0 * M * N * K;
+      if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+      SM_CHECK(gemm_oz(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc));
+      if (ctx.timing) {
+        SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+        SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
+        float ms = 0.f;
+        SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+        ctx.stats.gemm_oz_ms += ms;
+      }
+      return SM_OK;
+    }
+  }
   ctx.stats.gemm_launches += 1;
   ctx.stats.gemm_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
   const int nz = splitk_slices(M, N, K, std::max(1, ctx.num_sms));
@@ -339,12 +363,14 @@ int gemm_ctx_f32(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int 
       if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
       SM_CHECK(gemm_tc(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc));
       ctx.stats.gemm_tc_launches += 1;
+      ctx.stats.gemm_tc_flops += 2.0 * M * N * K;
       if (ctx.timing) {
         SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
         SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
         float ms = 0.f;
         SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
         ctx.stats.gemm32_ms += ms;
+        ctx.stats.gemm_tc_ms += ms;
       }
       return SM_OK;
     }
@@ -389,6 +415,11 @@ template int gemm_ctx_f32<cplx>(Ctx&, cudaStream_t, int, int, int, int, int, cpl
 
 template int gemm_ctx<double>(Ctx&, cudaStream_t, int, int, int, int, int, double, const double*,
                               int, const double*, int, double, double*, int);
+template int gemm_ctx_sel<double>(Ctx&, cudaStream_t, int, int, int, int, int, double,
+                                  const double*, int, const double*, int, double, double*, int,
+                                  bool);
+template int gemm_ctx_sel<cplx>(Ctx&, cudaStream_t, int, int, int, int, int, cplx, const cplx*,
+                                int, const cplx*, int, cplx, cplx*, int, bool);
 template int gemm_ctx<cplx>(Ctx&, cudaStream_t, int, int, int, int, int, cplx, const cplx*, int,
                             const cplx*, int, cplx, cplx*, int);
 

@@ -32,6 +32,7 @@ struct Ctx {
   // driver), the previous split's kept rank and leading singular values,
   // the model, and the recorder (features, kept rank) of every split
   bool contract32 = false;  // mixed forms: sweep contractions in FP32 arithmetic
+  bool fp64_tc = true;      // mixed forms: FP64 products on the tensor cores (gemm_oz)
   int split_site = -1, split_n = 0;
   int prev_rank = 0;
   std::vector<double> prev_s;
@@ -96,6 +97,10 @@ enum { OUT_VT = 1, OUT_SVT = 2 };
 template <typename T>
 int gemm_ctx(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A,
              int lda, const T* B, int ldb, T beta, T* C, int ldc);
+// allow_tc = false keeps the product on the FP64 SIMT kernel in every mode
+template <typename T>
+int gemm_ctx_sel(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha,
+                 const T* A, int lda, const T* B, int ldb, T beta, T* C, int ldc, bool allow_tc);
 template <typename T>
 int gemm(cudaStream_t st, int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda,
          const T* B, int ldb, T beta, T* C, int ldc);
@@ -115,6 +120,14 @@ int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, do
             const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc);
 int tc_status(Ctx& ctx, unsigned int** out);
 int tc_status_check(Ctx& ctx, cudaStream_t st);
+
+// --- gemm_oz.cu -------------------------------------------------------------
+// Real GEMM at FP64 accuracy on the BF16 tensor cores (error-free slicing of
+// the operands into 7-bit integer slices); gemm_ctx<double> uses it in the
+// mixed forms (ctx.fp64_tc) for shapes gemm_oz_eligible accepts.
+bool gemm_oz_eligible(int M, int N, int K);
+int gemm_oz(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
+            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc);
 
 // --- mps_ops.cu ------------------------------------------------------------
 template <typename T>

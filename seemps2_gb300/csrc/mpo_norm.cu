@@ -146,6 +146,7 @@ int mpo_scprod_impl(Ctx& ctx, cudaStream_t st, int L, const int* dout, const int
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
   out[0] = h[0];
   out[1] = sizeof(T) == sizeof(double) ? 0.0 : h[1];
+  if (ctx.precision != SM_PRECISION_FP64) SM_CHECK(tc_status_check(ctx, st));
   return SM_OK;
 }
 

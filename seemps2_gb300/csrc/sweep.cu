@@ -494,10 +494,11 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
       const int rc2 = rc == SM_OK ? w.estimate(c, &nm, &sc) : rc;
       ctx.contract32 = true;
       SM_CHECK(rc2);
-      SM_CHECK(tc_status_check(ctx, st));
       err = 2.0 * std::fabs(1.0 - sc / std::sqrt(nm * norm_state_sqr));
       if (rep->sweeps >= 1 && rep->sweeps <= 64) rep->sweep_err[rep->sweeps - 1] = err;
     }
+    // a tensor-core pipeline wait that timed out (none expected) fails the call
+    if (ctx.precision != SM_PRECISION_FP64) SM_CHECK(tc_status_check(ctx, st));
     double state_error = 0.0;
     for (int t = 0; t < w.nt; ++t) state_error += w.wabs[t] * w.term_err[t];
     double bound = state_error + std::sqrt(err);

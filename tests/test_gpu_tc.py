@@ -88,3 +88,78 @@ def test_fp32_contractions_of_a_sum():
     assert stats["gemm_tc_launches"] > 10, stats["gemm_tc_launches"]
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-10, fe
+
+
+def _gemm_fp64(opA, opB, A, B, M, N, K):
+    Ad = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    Bd = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    Cd = torch.empty((M, N), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.load().sm_gemm(
+        _lib.context(), _lib.SM_FLOAT64, OPS[opA], OPS[opB], M, N, K, C.c_void_p(Ad.data_ptr()),
+        A.shape[1], C.c_void_p(Bd.data_ptr()), B.shape[1], C.c_void_p(Cd.data_ptr()), N,
+        _lib.stream_handle()))
+    torch.cuda.synchronize()
+    return Cd.cpu().numpy()
+
+
+def _gemm_f64tc(opA, opB, A, B, M, N, K):
+    Ad = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    Bd = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    Cd = torch.empty((M, N), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.load().sm_gemm_f64tc(
+        _lib.context(), _lib.SM_FLOAT64, OPS[opA], OPS[opB], M, N, K, C.c_void_p(Ad.data_ptr()),
+        A.shape[1], C.c_void_p(Bd.data_ptr()), B.shape[1], C.c_void_p(Cd.data_ptr()), N,
+        _lib.stream_handle()))
+    torch.cuda.synchronize()
+    return Cd.cpu().numpy()
+
+
+@pytest.mark.parametrize("M,N,K,opA,opB", [
+    (128, 64, 256, "N", "N"),     # one tile, one exact chunk
+    (512, 512, 768, "N", "T"),    # three chunks, split-K
+    (225, 225, 512, "C", "N"),    # refinement Gram shape, ragged tiles
+    (300, 200, 100, "T", "T"),    # K not a multiple of 32
+    (64, 96, 1536, "N", "C"),     # deep K: six chunks over split-K
+])
+def test_fp64_tensor_core_gemm_has_fp64_accuracy(M, N, K, opA, opB):
+    """Error against numpy's FP64 product, normalised by |A||B| (the scale of
+    the FP64 GEMM error bound), within 8 sqrt(K) u and within twice the FP64
+    SIMT GEMM's own error (at least sqrt(K) u) on the same inputs; rows and columns scaled over
+    1e-8 .. 1e8, one zero row."""
+    rng = np.random.default_rng(M + 3 * N + 5 * K)
+    Aop = rng.normal(size=(M, K)) * np.exp(rng.uniform(-18, 18, size=(M, 1)))
+    Bop = rng.normal(size=(K, N)) * np.exp(rng.uniform(-18, 18, size=(1, N)))
+    Aop[M // 2] = 0.0
+    A = Aop if opA == "N" else Aop.T.copy()
+    B = Bop if opB == "N" else Bop.T.copy()
+    _lib.stats_reset()
+    out = _gemm_f64tc(opA, opB, A, B, M, N, K)
+    assert _lib.stats_read()["gemm_oz_launches"] == 1
+    native = _gemm_fp64(opA, opB, A, B, M, N, K)
+    ref = Aop @ Bop
+    scale = np.abs(Aop) @ np.abs(Bop)
+    scale = np.where(scale > 0, scale, 1.0)
+    err = np.max(np.abs(out - ref) / scale)
+    err_native = np.max(np.abs(native - ref) / scale)
+    assert err < 8 * np.sqrt(K) * 2.0**-53, err
+    # as accurate as an FP64 GEMM (whose own error can be 0 when it sums in
+    # numpy's order, hence the sqrt(K) u floor)
+    assert err <= 2 * max(err_native, np.sqrt(K) * 2.0**-53), (err, err_native)
+    assert np.all(out[M // 2] == 0.0)
+
+
+def test_fp64_tensor_core_gemm_cancellation():
+    """A product with heavy cancellation (result far below |A||B|): the error
+    stays at the FP64 level of |A||B|, as for an FP64 GEMM."""
+    rng = np.random.default_rng(11)
+    M, N, K = 256, 128, 512
+    A = rng.normal(size=(M, K))
+    X = rng.normal(size=(K, N))
+    B = X - A.T @ np.linalg.solve(A @ A.T + 1e-3 * np.eye(M), A @ X)  # nearly A-orthogonal
+    out = _gemm_f64tc("N", "N", A, B, M, N, K)
+    native = _gemm_fp64("N", "N", A, B, M, N, K)
+    ref = A @ B
+    scale = np.abs(A) @ np.abs(B)
+    err = np.max(np.abs(out - ref) / scale)
+    assert err < 8 * np.sqrt(K) * 2.0**-53
+    assert err <= 2 * max(np.max(np.abs(native - ref) / scale), np.sqrt(K) * 2.0**-53)
