@@ -126,6 +126,29 @@ __global__ void __launch_bounds__(NT) k_gemm(int opA, int opB, int M, int N, int
 }
 
 // C = alpha * sum_z part[z] + beta * C, slices summed in order z = 0, 1, ...
+// Small products (M N K below 2 Mi multiply-adds: the chain-end
+// contractions and the small splits' refinements): one thread per output
+// element, blocks of 64 threads along N so that even a 64 x 64 output spreads
+// over 64 SMs; GB300's FP64 rate per SM (~2 FMA per cycle) makes spreading the
+// work, not reusing it, what matters at these sizes.
+template <typename T>
+__global__ void __launch_bounds__(64) k_gemm_small(int opA, int opB, int M, int N, int K, T alpha,
+                                                   const T* __restrict__ A, int lda,
+                                                   const T* __restrict__ B, int ldb, T beta,
+                                                   T* __restrict__ C, int ldc) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (n >= N) return;
+  T acc = S<T>::zero();
+  for (int k = 0; k < K; ++k) {
+    const T a = load_op(opA == SM_OP_N ? A + (size_t)m * lda + k : A + (size_t)k * lda + m, opA);
+    const T b = load_op(opB == SM_OP_N ? B + (size_t)k * ldb + n : B + (size_t)n * ldb + k, opB);
+    acc = S<T>::fma(a, b, acc);
+  }
+  T* c = C + (size_t)m * ldc + n;
+  const bool zero_beta = S<T>::abs2(beta) == 0.0;
+  *c = zero_beta ? alpha * acc : alpha * acc + beta * *c;
+}
+
 template <typename T>
 __global__ void k_splitk_reduce(int M, int N, int nz, const T* __restrict__ part, T alpha, T beta,
                                 T* __restrict__ C, int ldc) {
@@ -333,6 +356,21 @@ int gemm_ctx_sel(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int 
   }
   ctx.stats.gemm_launches += 1;
   ctx.stats.gemm_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
+  if ((double)M * N * K <= 2.0 * 1024 * 1024 && M <= 65535) {
+    if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+    k_gemm_small<T><<<dim3((N + 63) / 64, M), 64, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb,
+                                                           beta, C, ldc);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    if (ctx.timing) {
+      SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+      SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
+      float ms = 0.f;
+      SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+      ctx.stats.gemm_ms += ms;
+    }
+    return SM_OK;
+  }
   const int nz = splitk_slices(M, N, K, std::max(1, ctx.num_sms));
   T* part = nullptr;
   if (nz > 1) SM_CHECK(ctx.scratch("gemm.splitk", (size_t)nz * M * N, &part));

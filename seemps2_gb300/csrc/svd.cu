@@ -497,24 +497,6 @@ __global__ void k_truncate(const double* s, int N, sm_strategy st, double* error
   }
 }
 
-// Mixed-form bookkeeping on the sorted values s (cnt of them) and the kept
-// rank D: the discarded weight |A|^2 - sum_{j<D} s_j^2 into res->err2,
-// info[2] = s[0], info[3] = s[D-1] for the host's checks and info[7] =
-// |A|^2 - sum of all cnt values^2, the weight outside the rows' span (what a
-// capped QR left behind).  |A|^2 is info[0].  One thread.
-__device__ void mixed_info(const double* s, int cnt, int D, SplitResult* res, double* info) {
-  double kept_D = 0.0, kept_all = 0.0;
-  for (int j = 0; j < cnt; ++j) {
-    if (j == D) kept_D = kept_all;
-    kept_all += s[j] * s[j];
-  }
-  if (D >= cnt) kept_D = kept_all;
-  res->err2 = fmax(0.0, info[0] - kept_D);
-  info[2] = s[0];
-  info[3] = s[max(D, 1) - 1];
-  info[7] = fmax(0.0, info[0] - kept_all);
-}
-
 // Rank sort of the k non-negative keys (descending, stable by index) by k
 // threads; writes perm, s_sorted (global) and ss (shared, may alias).
 __device__ void rank_sort(const unsigned long long* keys, int k, int* perm, double* s_sorted,
@@ -533,13 +515,13 @@ __device__ void rank_sort(const unsigned long long* keys, int k, int* perm, doub
   }
 }
 
-// Sort the k norms descending (stable by index), then truncate.  With
-// `staged` the sorted values and the error table live in shared memory while
-// the one-thread truncation rule runs over them (dynamic shared memory
-// 24 k + 8 bytes instead of 8 k); `info` (optional) also gets mixed_info.
+// Sort the k norms descending (stable by index), then truncate with the
+// reference rule.  With `staged` the sorted values and the error table live in
+// shared memory while the one-thread truncation rule runs over them (dynamic
+// shared memory 24 k + 8 bytes instead of 8 k).
 __global__ void k_sort_truncate(const double* nrm, int k, sm_strategy st, int* perm,
                                 double* s_sorted, double* errors, const JacobiCtl* ctl,
-                                SplitResult* res, int staged, double* info) {
+                                SplitResult* res, int staged) {
   extern __shared__ unsigned long long keys[];
   double* ss = staged ? reinterpret_cast<double*>(keys + k) : s_sorted;
   double* er = staged ? ss + k : errors;
@@ -559,7 +541,6 @@ __global__ void k_sort_truncate(const double* nrm, int k, sm_strategy st, int* p
     // non-finite input shows up as a NaN norm
     for (int i = 0; i < k; ++i)
       if (!(ss[i] == ss[i]) || ss[i] > DBL_MAX) res->status |= DEV_NONFINITE;
-    if (info) mixed_info(ss, k, D, res, info);
   }
   if (staged) {
     __syncthreads();
@@ -571,7 +552,7 @@ __global__ void k_sort_truncate(const double* nrm, int k, sm_strategy st, int* p
 // memory when 24 k + 8 bytes fit.
 static int sort_truncate(cudaStream_t st, const double* nrm, int k, const sm_strategy& strat,
                          int* perm, double* s_sorted, double* errors, const JacobiCtl* ctl,
-                         SplitResult* res, double* info = nullptr) {
+                         SplitResult* res) {
   constexpr size_t kLimit = 200 * 1024;
   const size_t keys = sizeof(unsigned long long) * (size_t)k;
   const size_t full = keys + sizeof(double) * (2 * (size_t)k + 1);
@@ -585,7 +566,7 @@ static int sort_truncate(cudaStream_t st, const double* nrm, int k, const sm_str
     SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
   k_sort_truncate<<<1, 1024, smem, st>>>(nrm, k, strat, perm, s_sorted, errors, ctl, res,
-                                         staged ? 1 : 0, info);
+                                         staged ? 1 : 0);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   return SM_OK;
@@ -1208,24 +1189,119 @@ __global__ void k_ns_matrix(const T* __restrict__ M, int k, T* __restrict__ F) {
   }
 }
 
+// Block-wide (blockDim.x = 1024 >= n) inclusive prefix sums P[i] = sum_{j<=i}
+// s[j]^2 in a fixed order (warp shuffles, then the warp totals): deterministic.
+__device__ void block_prefix_sq(const double* s, int n, double* P, double* wsum) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  double v = t < n ? s[t] * s[t] : 0.0;
+  for (int o = 1; o < 32; o <<= 1) {
+    const double u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  if (lane == 31) wsum[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double x = wsum[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const double u = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += u;
+    }
+    wsum[lane] = x;  // inclusive scan of the warp totals
+  }
+  __syncthreads();
+  if (t < n) P[t] = v + (w ? wsum[w - 1] : 0.0);
+  __syncthreads();
+}
+
+// Rank and bookkeeping of a mixed split from its n sorted values ss (shared)
+// and their prefix sums P (shared), all 1024 threads.  Relative-norm-squared
+// rule with exact weights (exact_rule): D = the smallest rank whose discarded
+// weight |A|^2 - P[D-1] is at most tol |A|^2 (|A|^2 = info[0], summed in FP64
+// from A itself); the singular-value rules: the first i >= 1 with s_i at or
+// below tol s_0 (relative) or tol (absolute); D is clamped to [1,
+// max_bond_dimension] (cython/truncation.pxi:251-327 states the same
+// contracts through the sorted values).  Writes res (D, err2 = |A|^2 -
+// P[D-1], status from ctl plus non-finite values), info[2] = s_0, info[3] =
+// s_{D-1} and info[7] = |A|^2 - P[n-1] (the weight outside the rows' span);
+// returns D to every thread.
+__device__ int mixed_rank_block(const double* ss, const double* P, int n, const sm_strategy& st,
+                                int exact_rule, const JacobiCtl* ctl, SplitResult* res,
+                                double* info, int* shD, int* shBad) {
+  const int t = threadIdx.x;
+  const int maxb = st.max_bond_dimension;
+  const double total = info[0];
+  if (t == 0) {
+    *shD = 0x7fffffff;
+    *shBad = 0;
+  }
+  __syncthreads();
+  if (t < n) {
+    bool cand = false;
+    int D = 0;
+    if (st.method == SM_DO_NOT_TRUNCATE) {
+    } else if (exact_rule) {
+      cand = total - P[t] <= st.tolerance * total;
+      D = t + 1;
+    } else {
+      const double max_error =
+          st.method == SM_RELATIVE_SINGULAR_VALUE ? st.tolerance * ss[0] : st.tolerance;
+      cand = t >= 1 && ss[t] <= max_error;
+      D = t;
+    }
+    if (cand) atomicMin(shD, D);
+    if (!(ss[t] == ss[t]) || ss[t] > DBL_MAX) atomicOr(shBad, 1);
+  }
+  __syncthreads();
+  int D = *shD == 0x7fffffff ? n : *shD;
+  D = max(1, min(D, maxb));
+  if (t == 0) {
+    res->D = D;
+    res->err2 = fmax(0.0, total - (D <= n ? P[D - 1] : P[n - 1]));
+    res->status = (ctl ? ctl->status : 0) | (*shBad ? DEV_NONFINITE : 0);
+    res->sweeps = ctl ? ctl->sweeps : 0;
+    info[2] = ss[0];
+    info[3] = ss[min(D, n) - 1];
+    info[7] = fmax(0.0, total - P[n - 1]);
+  }
+  return D;
+}
+
+// First step of a mixed split, one CTA of 1024 threads (n <= 1024): the FP32
+// rows' norms sorted descending (perm, s_sorted) and mixed_rank_block on them
+// (the host uses info[2], info[3] and the status).  Dynamic shared memory:
+// 24 n bytes.
+__global__ void __launch_bounds__(1024) k_mixed_sort(const double* __restrict__ nrm, int n,
+                                                     sm_strategy st, int exact_rule,
+                                                     const JacobiCtl* ctl, int* perm,
+                                                     double* s_sorted, SplitResult* res,
+                                                     double* info) {
+  extern __shared__ unsigned long long keys[];
+  double* ss = reinterpret_cast<double*>(keys + n);
+  double* P = ss + n;
+  __shared__ double wsum[32];
+  __shared__ int shD, shBad;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    keys[i] = (unsigned long long)__double_as_longlong(nrm[i]);
+  __syncthreads();
+  rank_sort(keys, n, perm, s_sorted, ss);
+  __syncthreads();
+  block_prefix_sq(ss, n, P, wsum);
+  mixed_rank_block(ss, P, n, st, exact_rule, ctl, res, info, &shD, &shBad);
+}
+
 // Final step of a mixed split, one CTA of 1024 threads, on G = C^H C of the
 // refined rows (C = W V^H, kw x cnt):
-//  * s_j = |C[:, j]| = sqrt(G_jj), sorted descending (perm) and truncated by
-//    the strategy's rule (status and sweeps from the cluster's ctl);
-//  * relative-norm-squared rule (exact_rule): D = the smallest rank whose
-//    discarded weight |A|^2 - sum_{j<D} s_j^2 is at most tol |A|^2, clamped to
-//    max_bond_dimension.  The weights are exact: s_j^2 are Rayleigh quotients
-//    of orthonormal rows and |A|^2 (info[0]) was summed in FP64 from A itself
-//    (cython/truncation.pxi:251-287 states the same contract through the
-//    sorted singular values);
-//  * mixed_info (err2, info[2], info[3], info[7]);
+//  * s_j = |C[:, j]| = sqrt(G_jj), sorted descending (perm);
+//  * mixed_rank_block: the rank (exact weights for the relative-norm rule:
+//    s_j^2 are Rayleigh quotients of orthonormal rows), err2, status, info[2],
+//    info[3], info[7];
 //  * coupling check, info[4]: the largest state change left by the coupling
 //    between a kept row i and a dropped row j, angle |G_ij| / (lambda_i -
 //    lambda_j) (lambda = s^2) times s_i / |A|_F; its square bounds the
 //    fidelity error the split can add.  Pairs whose both values lie below the
 //    FP32 resolution (s < blind s_0) are skipped: which of two unresolved
 //    directions is kept does not matter once the kept weight is exact.
-// Dynamic shared memory: 24 cnt + 8 bytes.
+// Dynamic shared memory: 24 cnt bytes.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_mixed_final(const T* __restrict__ G, int cnt,
                                                       sm_strategy st, int exact_rule, double blind,
@@ -1234,9 +1310,9 @@ __global__ void __launch_bounds__(1024) k_mixed_final(const T* __restrict__ G, i
                                                       SplitResult* res, double* info) {
   extern __shared__ unsigned long long keys[];
   double* ss = reinterpret_cast<double*>(keys + cnt);
-  double* er = ss + cnt;
+  double* P = ss + cnt;
   __shared__ double red[32];
-  __shared__ int Dsh;
+  __shared__ int shD, shBad;
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
     const double g = fmax(0.0, S<T>::real(G[(size_t)i * cnt + i]));
     keys[i] = (unsigned long long)__double_as_longlong(sqrt(g));
@@ -1244,34 +1320,9 @@ __global__ void __launch_bounds__(1024) k_mixed_final(const T* __restrict__ G, i
   __syncthreads();
   rank_sort(keys, cnt, perm, s_sorted, ss);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int D;
-    double e;
-    truncate_rule(ss, cnt, st, er, &D, &e);
-    res->status = ctl->status;
-    res->sweeps = ctl->sweeps;
-    for (int i = 0; i < cnt; ++i)
-      if (!(ss[i] == ss[i]) || ss[i] > DBL_MAX) res->status |= DEV_NONFINITE;
-    if (exact_rule) {
-      const double total = info[0];
-      const double allowed = st.tolerance * total;
-      double kept = 0.0;
-      D = cnt;
-      for (int j = 0; j < cnt; ++j) {
-        kept += ss[j] * ss[j];
-        if (total - kept <= allowed) {
-          D = j + 1;
-          break;
-        }
-      }
-      D = max(1, min(D, st.max_bond_dimension));
-    }
-    res->D = D;
-    mixed_info(ss, cnt, D, res, info);
-    Dsh = D;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i <= cnt; i += blockDim.x) errors[i] = er[i];
+  block_prefix_sq(ss, cnt, P, red);
+  const int Dsh = mixed_rank_block(ss, P, cnt, st, exact_rule, ctl, res, info, &shD, &shBad);
+  (void)errors;
   const int D = Dsh;
   const double sb = blind * ss[0];
   const double rnorm = info[0] > 0.0 ? 1.0 / sqrt(info[0]) : 0.0;
@@ -1396,7 +1447,11 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // FP32 singular values: sorted, and the rank the rule gives on them; for the
   // singular-value rules a cut below the FP32 resolution sends the split to
   // the FP64 path right away
-  SM_CHECK(sort_truncate(st, nrm, kcap, strat, perm, s_sorted, errors, ctl, res, info));
+  const bool exact_rule = strat.method == SM_RELATIVE_NORM_SQUARED_ERROR;
+  k_mixed_sort<<<1, 1024, 3 * sizeof(double) * (size_t)kcap, st>>>(
+      nrm, kcap, strat, exact_rule ? 1 : 0, ctl, perm, s_sorted, res, info);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
   Head* h = reinterpret_cast<Head*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(&h->c, ctl, sizeof(JacobiCtl), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaMemcpyAsync(h->info, info, 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1412,7 +1467,6 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     ctx.stats.cluster_ms += ms;
   }
   ctx.stats.jacobi_sweeps += hc.sweeps;
-  const bool exact_rule = strat.method == SM_RELATIVE_NORM_SQUARED_ERROR;
   if (hc.status != 0 || (!exact_rule && h->info[3] < kMixedBlind * h->info[2])) {
     ctx.stats.mixed_fallbacks += 1;
     ctx.stats.mixed_fallback_fp32 += 1;
@@ -1472,7 +1526,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // 3. singular values, truncation, exact discarded weight
   SM_CHECK(w_vh(V, Cb));
   SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
-  const size_t fin_smem = sizeof(double) * (3 * (size_t)cnt + 1);
+  const size_t fin_smem = sizeof(double) * 3 * (size_t)cnt;
   if (fin_smem > 48 * 1024)
     SM_CUDA_CHECK(cudaFuncSetAttribute(k_mixed_final<T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fin_smem));
