@@ -263,6 +263,77 @@ def run_split_case(args):
     print(json.dumps(out), flush=True)
 
 
+def make_batch_workload(count: int, seed: int = SEED + 4):
+    """The batching configuration: `count` independent random MPS, complex64 storage, lengths
+    n ~ U[10, 40], d = 2, uniform bond chi from {8, 16, 32, 64, 128} (i.i.d. complex normal,
+    normalised), each with its own random complex MPO of bond D in {2, 4} (entries / sqrt(D d))."""
+    from oracle import seemps_oracle as so
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.integers(10, 41))
+        chi = int(rng.choice([8, 16, 32, 64, 128]))
+        D = int(rng.choice([2, 4]))
+        mps = so.random_mps(2, n, chi, rng, complex_=True)
+        nrm = np.sqrt(abs(so.scprod(mps, mps)))
+        mps[0] = mps[0] / nrm
+        mpo = so.random_mpo(2, n, D, rng, complex_=True)
+        out.append(([t.astype(np.complex64) for t in mps], [t.astype(np.complex64) for t in mpo], chi))
+    return out
+
+
+def run_batch(args):
+    """Batched compression: `--batch-count` instances (see make_batch_workload), each MPO.apply +
+    simplify to tolerance 1e-8 with max bond = the instance's own chi (the product, bond chi D, is
+    compressed back to chi), 2 sweeps, FP64 truncation decisions.  The stream autotuner picks the
+    number of instances in flight on a 64-instance sample; the whole batch is then timed with it and
+    with one instance at a time.  Reports MPS/s and p50 / p99 per-instance latency."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import seemps2_gb300 as sg
+    from seemps2_gb300 import batch
+
+    inst = make_batch_workload(args.batch_count)
+    mpos = [sg.MPO(mpo, sg.DEFAULT_STRATEGY.replace(tolerance=1e-8, max_bond_dimension=chi,
+                                                    max_sweeps=2, simplification_tolerance=0.0))
+            for mps, mpo, chi in inst]
+    states = [sg.MPS(mps) for mps, mpo, chi in inst]
+    precision = {"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed"}[args.form]
+    best, table = batch.tune_streams(mpos, states, sample=64, precision=precision)
+    res, rep = batch.apply_batch(mpos, states, streams=best, precision=precision)
+    _, rep1 = batch.apply_batch(mpos, states, streams=1, precision=precision)
+    check = None
+    if not args.no_cpu:
+        from oracle import seemps_oracle as so
+
+        worst = 0.0
+        for (mps, mpo, chi), out in list(zip(inst, res))[:8]:
+            ref = so.mpo_apply([t.astype(np.complex128) for t in mpo],
+                               [t.astype(np.complex128) for t in mps],
+                               so.DEFAULT_STRATEGY.replace(tolerance=1e-8, max_bond_dimension=chi,
+                                                           max_sweeps=2,
+                                                           simplification_tolerance=0.0))
+            fe = so.fidelity_error([x.detach().cpu().numpy() for x in out._data], ref.tensors)
+            worst = max(worst, float(fe))
+        check = {"instances_checked": 8, "max_fidelity_error_vs_oracle": worst}
+    sizes = [(len(m), chi) for m, _, chi in inst]
+    print(json.dumps({
+        "metric": "batched MPO.apply+simplify, MPS/s", "value": rep.instances_per_s, "unit": "MPS/s",
+        "higher_is_better": True, "n_gpus": 1, "form": args.form,
+        "config": {"workload": f"{len(inst)} MPS, n~U[10,40], chi in {{8..128}}, D in {{2,4}}, "
+                               "complex64 storage, tol 1e-8, max bond = chi, 2 sweeps",
+                   "sites_total": sum(n for n, _ in sizes)},
+        "streams": best, "autotune_instances_per_s": table,
+        "p50_s": rep.percentile(50), "p99_s": rep.percentile(99), "wall_s": rep.wall_s,
+        "one_in_flight": rep1.summary(), "speedup_vs_one_in_flight":
+            rep.instances_per_s / rep1.instances_per_s if rep1.instances_per_s else None,
+        "oracle_check": check}), flush=True)
+
+
 def run_gemm_case(args):
     """One real M x N x K product (op N, N) timed with CUDA events: the FP64 SIMT
     GEMM, the tensor-core 3xTF32 GEMM (FP32 accuracy) and the FP64-accurate
@@ -338,6 +409,9 @@ def main():
     ap.add_argument("--gemm-case", type=int, nargs=3, metavar=("M", "N", "K"),
                     help="time one real M x N x K product on the tensor cores (3xTF32) and as "
                          "the FP64 GEMM, and exit")
+    ap.add_argument("--batch", action="store_true",
+                    help="batched compression of many independent MPS (MPS/s, p50/p99) and exit")
+    ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--profile-step", action="store_true",
                     help="after the warm-up, run one step of --form between cudaProfilerStart "
                          "and cudaProfilerStop (for ncu --profile-from-start off) and exit")
@@ -346,6 +420,8 @@ def main():
         return run_split_case(args)
     if args.gemm_case:
         return run_gemm_case(args)
+    if args.batch:
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
 

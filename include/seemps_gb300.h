@@ -179,6 +179,14 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
 int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
                   const void* A, int lda, const void* B, int ldb, void* C, int ldc,
                   void* stream);
+/* Marks a context whose calls run concurrently with other streams' work on the
+ * same device (several host threads, each with its own context and stream):
+ * the FP64 SVD's grid-barrier kernels (Householder QR, Jacobi) then run as one
+ * CTA, since a multi-CTA grid barrier can wait indefinitely for CTAs that other
+ * streams' kernels keep from being resident (its bounded spin then reports
+ * SM_ERR_TIMEOUT).  seemps2_gb300.batch sets it on its worker contexts. */
+int sm_ctx_set_concurrent(void* ctx, int on);
+
 /* FP64 products of the mixed forms (state norm, refinement, final estimate,
  * FP64 contractions): 1 (default) on the tensor cores as sm_gemm_f64tc, 0 on
  * the FP64 SIMT kernel.  SM_PRECISION_FP64 always uses the SIMT kernel. */

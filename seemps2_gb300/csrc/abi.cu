@@ -1,6 +1,8 @@
 // extern "C" boundary of libseemps_gb300.so (declared in include/seemps_gb300.h).
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <string>
 
@@ -26,6 +28,29 @@ int scprod_impl(Ctx&, cudaStream_t, int, const int*, const int*, const void* con
 static thread_local std::string g_error;
 static std::atomic<long long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int coop_launch(const void* fn, dim3 grid, dim3 block, void** args, cudaStream_t st) {
+  if (grid.x * grid.y * grid.z == 1) {  // one CTA: its barrier waits for no one
+    SM_CUDA_CHECK(cudaLaunchCooperativeKernel(fn, grid, block, args, 0, st));
+    return SM_OK;
+  }
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  SM_CUDA_CHECK(cudaLaunchCooperativeKernel(fn, grid, block, args, 0, st));
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  return SM_OK;
+}
+
+int raise_smem_limit(const void* fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<const void*, size_t> limit;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = limit[fn];
+  if (bytes <= cur) return SM_OK;
+  SM_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+  return SM_OK;
+}
 long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 void set_error(const std::string& msg) { g_error = msg; }
 const char* last_error() { return g_error.c_str(); }
@@ -296,6 +321,12 @@ int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K, c
     return tc_status_check(c, s);
   }
   return sm_gemm(ctx, dtype, opA, opB, M, N, K, A, lda, B, ldb, C, ldc, stream);
+}
+
+int sm_ctx_set_concurrent(void* ctx, int on) {
+  SM_GUARD_CTX(ctx);
+  as_ctx(ctx)->concurrent = on != 0;
+  return SM_OK;
 }
 
 int sm_ctx_set_fp64_products(void* ctx, int tensor_cores) {

@@ -318,7 +318,11 @@ __global__ void __launch_bounds__(kOzThreads, 1)
           if (col < N) {
             const double acc = fma((double)S[j], 3.725290298461914e-09 /* 2^-28 */,
                                    (double)small[j]);
-            const double v = ldexp(acc, er + max(eb[col], -1100));
+            // 2^e from its exponent bits (one FP64 multiply; GB300's FP64 pipe
+            // makes ldexp's general path expensive), ldexp outside that range
+            const int e = er + max(eb[col], -1100);
+            const double v = (e > -1022 && e < 1024) ? acc * __hiloint2double((e + 1023) << 20, 0)
+                                                     : ldexp(acc, e);
             if (part) {
               part[((size_t)blockIdx.z * M + row) * N + col] = v;
             } else {
@@ -451,17 +455,17 @@ __global__ void k_oz_reduce(int M, int N, int nz, const double* __restrict__ par
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 oz_encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // looked up once (thread-safe static initialisation); null when unavailable
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    else
-      cudaGetLastError();
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
 }
 
@@ -528,12 +532,7 @@ int gemm_oz(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, do
   nz = (nslabs + slabs_per - 1) / slabs_per;
   double* part = nullptr;
   if (nz > 1) SM_CHECK(ctx.scratch("oz.part", (size_t)nz * M * N, &part));
-  static bool attr = false;
-  if (!attr) {
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kOzSmem));
-    attr = true;
-  }
+  SM_CHECK(raise_smem_limit(k_gemm_oz, kOzSmem));
   const dim3 grid((N + ON - 1) / ON, (M + OM - 1) / OM, nz);
   k_gemm_oz<<<grid, kOzThreads, kOzSmem, st>>>(mA, mB, ea, eb, M, N, nslabs, slabs_per, alpha,
                                                beta, C, ldc, part, status);

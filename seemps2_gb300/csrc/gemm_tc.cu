@@ -309,17 +309,17 @@ __global__ void k_tc_reduce(int M, int N, int nz, const double* __restrict__ par
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // looked up once (thread-safe static initialisation); null when unavailable
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    else
-      cudaGetLastError();
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
 }
 
@@ -385,12 +385,7 @@ int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, do
   nz = (ktiles + kt_per - 1) / kt_per;
   double* part = nullptr;
   if (nz > 1) SM_CHECK(ctx.scratch("tc.part", (size_t)nz * M * N, &part));
-  static bool attr = false;
-  if (!attr) {
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kTCSmem));
-    attr = true;
-  }
+  SM_CHECK(raise_smem_limit(k_gemm_tc, kTCSmem));
   const dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, nz);
   k_gemm_tc<<<grid, kTCThreads, kTCSmem, st>>>(mAh, mAl, mBh, mBl, M, N, ktiles, kt_per, alpha,
                                                beta, C, ldc, part, status);

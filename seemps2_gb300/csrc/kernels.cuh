@@ -33,6 +33,7 @@ struct Ctx {
   // the model, and the recorder (features, kept rank) of every split
   bool contract32 = false;  // mixed forms: sweep contractions in FP32 arithmetic
   bool fp64_tc = true;      // mixed forms: FP64 products on the tensor cores (gemm_oz)
+  bool concurrent = false;  // shares the device with other streams: no multi-CTA grid barriers
   int split_site = -1, split_n = 0;
   int prev_rank = 0;
   std::vector<double> prev_s;
@@ -61,6 +62,23 @@ struct Ctx {
     return scratch(name, count * sizeof(P), reinterpret_cast<void**>(out));
   }
 };
+
+// Raises kernel `fn`'s dynamic shared-memory limit to at least `bytes` (never
+// lowers it), under a process-wide lock: contexts on different host threads
+// launch the same kernels with different sizes concurrently.
+int raise_smem_limit(const void* fn, size_t bytes);
+template <typename K>
+int raise_smem_limit(K* fn, size_t bytes) {
+  return raise_smem_limit(reinterpret_cast<const void*>(fn), bytes);
+}
+
+// Cooperative (grid-barrier) launch on `st`.  A multi-CTA grid returns once
+// the kernel has completed, holding a process-wide lock meanwhile, so no two
+// such kernels of this process overlap.  That alone does not make a grid
+// barrier safe next to other streams' work (their kernels can keep the grid's
+// remaining CTAs from becoming resident): contexts that share the device set
+// `concurrent` and launch these kernels as one CTA.
+int coop_launch(const void* fn, dim3 grid, dim3 block, void** args, cudaStream_t st);
 
 // Kernel launches issued by this library in this process (all contexts).
 void note_launch(int n = 1);

@@ -562,9 +562,7 @@ static int sort_truncate(cudaStream_t st, const double* nrm, int k, const sm_str
     set_error("svd: matrix too large for the on-chip sort");
     return SM_ERR_VALUE;
   }
-  if (smem > 48 * 1024)
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+  if (smem > 48 * 1024) SM_CHECK(raise_smem_limit(k_sort_truncate, smem));
   k_sort_truncate<<<1, 1024, smem, st>>>(nrm, k, strat, perm, s_sorted, errors, ctl, res,
                                          staged ? 1 : 0);
   note_launch();
@@ -657,12 +655,14 @@ int launch_jacobi(Ctx& ctx, cudaStream_t st, T* Wx, int ld, int k, int l, int L,
     per_sm = std::max(1, per_sm);
     ctx.coop_blocks[key] = per_sm;
   }
-  const int grid = std::max(1, std::min(npairs, per_sm * sms));
+  // a context whose work shares the device with other streams runs the
+  // iteration as one CTA: its grid barrier then never waits for CTAs that
+  // other streams' kernels keep from being resident
+  const int grid = ctx.concurrent ? 1 : std::max(1, std::min(npairs, per_sm * sms));
   int ms = kMaxSweeps;
   void* args[] = {&Wx, &ld, &k, &l, &L, &tol2, &use_floor, &defl_rel, &defl_abs, &ms, &nrm,
                   &nrm0, &act, &ctl};
-  SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
-                                            dim3(kJacobiNT), args, 0, st));
+  SM_CHECK(coop_launch(reinterpret_cast<const void*>(fn), dim3(grid), dim3(kJacobiNT), args, st));
   note_launch();
   return SM_OK;
 }
@@ -954,13 +954,15 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
       per_sm = std::max(1, per_sm);
       ctx.coop_blocks[key] = per_sm;
     }
-    const int grid = std::max(1, std::min((l + QNT / 32 - 1) / (QNT / 32), per_sm * std::max(1, ctx.num_sms)));
+    const int grid =
+        ctx.concurrent
+            ? 1  // one CTA: no grid barrier to wait on (see run_jacobi)
+            : std::max(1, std::min((l + QNT / 32 - 1) / (QNT / 32), per_sm * std::max(1, ctx.num_sms)));
     SM_CHECK(ctx.scratch("svd.qpart", (size_t)grid, &qpart));
     SM_CUDA_CHECK(cudaMemsetAsync(qctl, 0, sizeof(QrCtl), st));
     int kk = kw, ll = l;
     void* args[] = {&Wt, &kk, &ll, &drel, &vbuf, &qpart, &qctl};
-    SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
-                                              dim3(QNT), args, 0, st));
+    SM_CHECK(coop_launch(reinterpret_cast<const void*>(fn), dim3(grid), dim3(QNT), args, st));
     note_launch();
     const size_t tot = (size_t)k * l;
     const int blocks = (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, 4096));
@@ -1527,9 +1529,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(w_vh(V, Cb));
   SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
   const size_t fin_smem = sizeof(double) * 3 * (size_t)cnt;
-  if (fin_smem > 48 * 1024)
-    SM_CUDA_CHECK(cudaFuncSetAttribute(k_mixed_final<T>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fin_smem));
+  if (fin_smem > 48 * 1024) SM_CHECK(raise_smem_limit(k_mixed_final<T>, fin_smem));
   k_mixed_final<T><<<1, 1024, fin_smem, st>>>(Gb, cnt, strat, exact_rule ? 1 : 0, kMixedBlind, ctl,
                                               perm, s_sorted, errors, res, info);
   note_launch();
@@ -1839,8 +1839,7 @@ int launch_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double t
   int L = l + k;
   void* args[] = {&Wx, &ld, &k, &l, &L, &tol2, &use_floor, &defl_rel, &defl_abs, &ms, &nrm,
                   &nrm0, &act, &ctl};
-  SM_CUDA_CHECK(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(grid),
-                                            dim3(kJacobiNT), args, 0, st));
+  SM_CHECK(coop_launch(reinterpret_cast<const void*>(fn), dim3(grid), dim3(kJacobiNT), args, st));
   note_launch();
   return SM_OK;
 }

@@ -542,8 +542,7 @@ bool cluster_config(int kw, int l, size_t* smem_out) {
   if (smem > 227 * 1024) return false;
   auto fn = k_split_cluster<T, E>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess) {
+      raise_smem_limit(fn, smem) != SM_OK) {
     cudaGetLastError();
     return false;
   }
