@@ -334,6 +334,74 @@ def run_batch(args):
         "oracle_check": check}), flush=True)
 
 
+def run_dmrg_matvec(args):
+    """The DMRG configuration's hot operation: the two-site effective-Hamiltonian matvec at
+    chi = 256 of a Heisenberg chain (MPO bond 5, d = 2), environments with i.i.d. normal entries
+    (the cost does not depend on their values), the two-site MPO of the chain's bulk.  Each
+    precision is timed over 50 matvecs with CUDA events and compared with the FP64 result; the
+    oracle's NumPy matvec is timed on the host cores; a 30-vector Lanczos run (FP64
+    re-orthogonalisation) is timed at FP64 and BF16."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from oracle import dmrg_oracle as do
+    from seemps2_gb300 import dmrg
+
+    chi, D, d = 256, 5, 2
+    rng = np.random.default_rng(SEED + 7)
+    W = do.heisenberg_mpo(8)
+    H = do.two_site_hamiltonian(W[3], W[4])
+    L = rng.normal(size=(chi, D, chi))
+    R = rng.normal(size=(chi, D, chi))
+    L = 0.5 * (L + L.transpose(2, 1, 0))
+    R = 0.5 * (R + R.transpose(2, 1, 0))
+    v = rng.normal(size=(chi, d, d, chi))
+    Ld, Hd, Rd, vd = (torch.from_numpy(x).cuda() for x in (L, H, R, v))
+    flops = 2.0 * chi * D * chi * d * d * chi * 2 + 2.0 * chi * chi * (D * d * d) ** 2
+    out = {"workload": f"two-site matvec, chi={chi}, MPO bond {D} (Heisenberg), d={d}",
+           "flops_per_matvec": flops}
+    ref = None
+    for prec in ("fp64", "fp64tc", "tf32x3", "bf16"):
+        o = torch.empty((chi, d, d, chi), dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            dmrg.two_site_matvec(Ld, Hd, Rd, vd, prec, out=o)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(50):
+            dmrg.two_site_matvec(Ld, Hd, Rd, vd, prec, out=o)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 50
+        res = o.cpu().numpy()
+        if ref is None:
+            ref = res
+        out[prec] = {"ms_per_matvec": ms, "matvecs_per_s": 1e3 / ms,
+                     "tflops": flops / (ms / 1e3) / 1e12,
+                     "rel_err_vs_fp64": float(np.linalg.norm(res - ref) / np.linalg.norm(ref))}
+    out["bf16"]["frac_of_bf16_peak"] = out["bf16"]["tflops"] / measured_bf16_tflops()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        do.two_site_matvec(L, H, R, v)
+    cpu_ms = (time.perf_counter() - t0) / reps * 1e3
+    out["cpu_oracle"] = {"ms_per_matvec": cpu_ms, "cores": os.cpu_count(),
+                         "kind": "port (NumPy, the reference's own reshape/GEMM sequence)"}
+    for prec in ("fp64", "bf16"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev, _, steps = dmrg.lanczos_ground_state(Ld, Hd, Rd, vd, krylov=30, precision=prec)
+        torch.cuda.synchronize()
+        out[f"lanczos_{prec}"] = {"s": time.perf_counter() - t0, "steps": steps, "eigenvalue": ev}
+    out["lanczos_bf16"]["rel_diff_vs_fp64"] = abs(out["lanczos_bf16"]["eigenvalue"] -
+                                                  out["lanczos_fp64"]["eigenvalue"]) / abs(
+        out["lanczos_fp64"]["eigenvalue"])
+    print(json.dumps(out), flush=True)
+
+
 def run_gemm_case(args):
     """One real M x N x K product (op N, N) timed with CUDA events: the FP64 SIMT
     GEMM, the tensor-core 3xTF32 GEMM (FP32 accuracy) and the FP64-accurate
@@ -409,6 +477,8 @@ def main():
     ap.add_argument("--gemm-case", type=int, nargs=3, metavar=("M", "N", "K"),
                     help="time one real M x N x K product on the tensor cores (3xTF32) and as "
                          "the FP64 GEMM, and exit")
+    ap.add_argument("--dmrg-matvec", action="store_true",
+                    help="time the DMRG two-site matvec (chi 256, MPO bond 5) per precision and exit")
     ap.add_argument("--batch", action="store_true",
                     help="batched compression of many independent MPS (MPS/s, p50/p99) and exit")
     ap.add_argument("--batch-count", type=int, default=512)
@@ -422,6 +492,8 @@ def main():
         return run_gemm_case(args)
     if args.batch:
         return run_batch(args)
+    if args.dmrg_matvec:
+        return run_dmrg_matvec(args)
     if args.impl == "reference":
         return run_reference(args)
 

@@ -167,6 +167,12 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
             const void* A, int lda, const void* B, int ldb, void* C, int ldc,
             void* stream);
 
+/* sm_gemm with scalars: C = alpha op(A) op(B) + beta C (alpha, beta as (re, im)
+ * pairs; beta = 0 does not read C).  FP64 SIMT kernel. */
+int sm_gemm_ex(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
+               const double* alpha, const void* A, int lda, const void* B, int ldb,
+               const double* beta, void* C, int ldc, void* stream);
+
 /* The same product at FP64 accuracy on the BF16 tensor cores (no reference
  * counterpart): real operands with M, N >= 32, K >= 32 and at least 2 Mi
  * multiply-adds are scaled by powers of two per row of op(A) / column of
@@ -301,6 +307,22 @@ int sm_mpo_scprod(void* ctx, int dtype, int L, const int* dout, const int* din,
                   const int* mpo_bonds, const void* const* mpo, const int* bra_bonds,
                   const void* const* bra, const int* ket_bonds, const void* const* ket,
                   double* out, void* stream);
+
+/* Two-site effective-Hamiltonian matvec of DMRG (QuadraticForm.two_site_operator
+ * ._matvec, operators/quadratic.py:187-237):
+ *   out[a, ko, lo, g] = sum L[a, c, b] v[b, k, l, f] H[c, ko, k, lo, l, e] R[g, e, f]
+ * with L (a, c, b) the left MPO environment (bra, MPO, ket), H (c, p1, p1, p2,
+ * p2, e) the two-site MPO (_contract_last_and_first of the two sites' MPO
+ * tensors), R (g, e, f) the right environment, v (b, p1, p2, f) and out (a,
+ * p1, p2, g).  dims = {a, c, b, p1, p2, e, g, f}.  precision: SM_MATVEC_FP64
+ * (SIMT FP64, the reference's arithmetic), SM_MATVEC_FP64TC (FP64-accurate on
+ * the BF16 tensor cores), SM_MATVEC_TF32X3 (FP32-accurate, 3xTF32) or
+ * SM_MATVEC_BF16 (one BF16 product, FP32 accumulation); real operands only on
+ * the tensor cores (complex ones use the SIMT kernels of the same accuracy
+ * class).  No reference counterpart for the reduced precisions. */
+enum { SM_MATVEC_FP64 = 0, SM_MATVEC_FP64TC = 1, SM_MATVEC_TF32X3 = 2, SM_MATVEC_BF16 = 3 };
+int sm_two_site_matvec(void* ctx, int dtype, const int* dims, const void* L, const void* H,
+                       const void* R, const void* v, void* out, int precision, void* stream);
 
 /* Upper bound on the bond dimensions a simplify of these kets can produce:
  * min(max_bond_dimension, summed ket bond); fills cap_bonds (L+1). */

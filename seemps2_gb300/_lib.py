@@ -104,10 +104,13 @@ SIGNATURES = {
                           vp, C.c_int, vp, C.c_int, vp]),
     "sm_gemm_f32": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp,
                               C.c_int, vp, C.c_int, vp, C.c_int, vp]),
+    "sm_gemm_ex": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp, vp,
+                             C.c_int, vp, C.c_int, dp, vp, C.c_int, vp]),
     "sm_gemm_f64tc": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp,
                                 C.c_int, vp, C.c_int, vp, C.c_int, vp]),
     "sm_ctx_set_fp64_products": (C.c_int, [vp, C.c_int]),
     "sm_ctx_set_concurrent": (C.c_int, [vp, C.c_int]),
+    "sm_two_site_matvec": (C.c_int, [vp, C.c_int, ip, vp, vp, vp, vp, vp, C.c_int, vp]),
     "sm_svd": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp]),
     "sm_left_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,
                                      vp, ip, dp, vp]),

@@ -303,6 +303,24 @@ int sm_gemm(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const v
                             false);
 }
 
+int sm_gemm_ex(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const double* alpha,
+               const void* A, int lda, const void* B, int ldb, const double* beta, void* C, int ldc,
+               void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (opA < 0 || opA > 2 || opB < 0 || opB > 2 || M < 0 || N < 0 || K < 0 || !alpha || !beta) {
+    set_error("sm_gemm_ex: invalid op flag, size or scalar");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return gemm_ctx_sel<double>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K, alpha[0],
+                                (const double*)A, lda, (const double*)B, ldb, beta[0], (double*)C,
+                                ldc, false);
+  return gemm_ctx_sel<cplx>(*as_ctx(ctx), as_stream(stream), opA, opB, M, N, K,
+                            cplx{alpha[0], alpha[1]}, (const cplx*)A, lda, (const cplx*)B, ldb,
+                            cplx{beta[0], beta[1]}, (cplx*)C, ldc, false);
+}
+
 int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K, const void* A,
                   int lda, const void* B, int ldb, void* C, int ldc, void* stream) {
   SM_GUARD_CTX(ctx);
@@ -321,6 +339,35 @@ int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K, c
     return tc_status_check(c, s);
   }
   return sm_gemm(ctx, dtype, opA, opB, M, N, K, A, lda, B, ldb, C, ldc, stream);
+}
+
+int sm_two_site_matvec(void* ctx, int dtype, const int* dims, const void* L, const void* H,
+                       const void* R, const void* v, void* out, int precision, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (!dims || !L || !H || !R || !v || !out || precision < SM_MATVEC_FP64 ||
+      precision > SM_MATVEC_BF16) {
+    set_error("two_site_matvec: null argument or unknown precision");
+    return SM_ERR_VALUE;
+  }
+  for (int i = 0; i < 8; ++i)
+    if (dims[i] <= 0) {
+      set_error("two_site_matvec: non-positive dimension");
+      return SM_ERR_VALUE;
+    }
+  Ctx& c = *as_ctx(ctx);
+  cudaStream_t s = as_stream(stream);
+  int rc;
+  if (dtype == SM_FLOAT64)
+    rc = two_site_matvec<double>(c, s, dims[0], dims[1], dims[2], dims[3], dims[4], dims[5],
+                                 dims[6], dims[7], (const double*)L, (const double*)H,
+                                 (const double*)R, (const double*)v, (double*)out, precision);
+  else
+    rc = two_site_matvec<cplx>(c, s, dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6],
+                               dims[7], (const cplx*)L, (const cplx*)H, (const cplx*)R,
+                               (const cplx*)v, (cplx*)out, precision);
+  SM_CHECK(rc);
+  return precision == SM_MATVEC_FP64 ? SM_OK : tc_status_check(c, s);
 }
 
 int sm_ctx_set_concurrent(void* ctx, int on) {

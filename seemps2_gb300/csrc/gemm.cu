@@ -22,6 +22,13 @@ namespace {
 
 constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
 
+__device__ __forceinline__ double shfl_xor_T(double v, int o) {
+  return __shfl_xor_sync(0xffffffffu, v, o);
+}
+__device__ __forceinline__ cplx shfl_xor_T(cplx v, int o) {
+  return cplx{__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o)};
+}
+
 template <typename T>
 __device__ __forceinline__ T load_op(const T* p, int op) {
   T v = __ldg(p);
@@ -147,6 +154,60 @@ __global__ void __launch_bounds__(64) k_gemm_small(int opA, int opB, int M, int 
   T* c = C + (size_t)m * ldc + n;
   const bool zero_beta = S<T>::abs2(beta) == 0.0;
   *c = zero_beta ? alpha * acc : alpha * acc + beta * *c;
+}
+
+// Matrix-vector shapes (N = 1, or M = 1): the Lanczos projections and norms.
+// N = 1, op(A) rows contiguous (op N): block (m, kb) sums K range kb of row m
+// into part[m * nkb + kb]; k_gemv_final adds the partials in order.
+template <typename T>
+__global__ void k_gemv_rows(int opB, const T* __restrict__ A, int lda, const T* __restrict__ B,
+                            int ldb, int K, int kchunk, T* __restrict__ part) {
+  __shared__ T red[32];
+  const int m = blockIdx.x, kb = blockIdx.y;
+  const int k0 = kb * kchunk, k1 = min(K, k0 + kchunk);
+  T acc = S<T>::zero();
+  for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    const T b = load_op(opB == SM_OP_N ? B + (size_t)k * ldb : B + k, opB);
+    acc = S<T>::fma(A[(size_t)m * lda + k], b, acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc = acc + shfl_xor_T(acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T t = S<T>::zero();
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = t + red[w];
+    part[(size_t)m * gridDim.y + kb] = t;
+  }
+}
+
+template <typename T>
+__global__ void k_gemv_final(int M, int nkb, const T* __restrict__ part, T alpha, T beta,
+                             T* __restrict__ C, int ldc) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  T acc = S<T>::zero();
+  for (int kb = 0; kb < nkb; ++kb) acc = acc + part[(size_t)m * nkb + kb];
+  T* c = C + (size_t)m * ldc;
+  *c = S<T>::abs2(beta) == 0.0 ? alpha * acc : alpha * acc + beta * *c;
+}
+
+// N = 1 with op(A) = A^T / A^H (A stored K x M) or M = 1: one thread per output
+// element, the K loop coalesced across threads.
+template <typename T>
+__global__ void k_gemv_cols(int opA, int opB, int M, int N, int K, T alpha,
+                            const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb,
+                            T beta, T* __restrict__ C, int ldc) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)M * N) return;
+  const int m = (int)(e / N), n = (int)(e % N);
+  T acc = S<T>::zero();
+  for (int k = 0; k < K; ++k) {
+    const T a = load_op(opA == SM_OP_N ? A + (size_t)m * lda + k : A + (size_t)k * lda + m, opA);
+    const T b = load_op(opB == SM_OP_N ? B + (size_t)k * ldb + n : B + (size_t)n * ldb + k, opB);
+    acc = S<T>::fma(a, b, acc);
+  }
+  T* c = C + (size_t)m * ldc + n;
+  *c = S<T>::abs2(beta) == 0.0 ? alpha * acc : alpha * acc + beta * *c;
 }
 
 template <typename T>
@@ -356,6 +417,26 @@ int gemm_ctx_sel(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int 
   }
   ctx.stats.gemm_launches += 1;
   ctx.stats.gemm_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
+  if (N == 1 && opA == SM_OP_N && K >= 1024 && M <= 65535) {
+    // long dot products: K split over blocks, partials summed in order
+    const int nkb = std::min(64, (K + 4095) / 4096);
+    const int kchunk = (K + nkb - 1) / nkb;
+    T* part;
+    SM_CHECK(ctx.scratch("gemv.part", (size_t)M * nkb, &part));
+    k_gemv_rows<T><<<dim3(M, nkb), 256, 0, st>>>(opB, A, lda, B, ldb, K, kchunk, part);
+    k_gemv_final<T><<<(M + 127) / 128, 128, 0, st>>>(M, nkb, part, alpha, beta, C, ldc);
+    note_launch(2);
+    SM_CUDA_CHECK(cudaGetLastError());
+    return SM_OK;
+  }
+  if ((N == 1 || M == 1) && K <= 4096) {
+    const size_t mn = (size_t)M * N;
+    k_gemv_cols<T><<<(unsigned)((mn + 127) / 128), 128, 0, st>>>(opA, opB, M, N, K, alpha, A, lda,
+                                                                   B, ldb, beta, C, ldc);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    return SM_OK;
+  }
   if ((double)M * N * K <= 2.0 * 1024 * 1024 && M <= 65535) {
     if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
     k_gemm_small<T><<<dim3((N + 63) / 64, M), 64, 0, st>>>(opA, opB, M, N, K, alpha, A, lda, B, ldb,

@@ -26,6 +26,7 @@
 #include <algorithm>
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include "kernels.cuh"
@@ -34,17 +35,28 @@ namespace sm {
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 32, TS = 3;
+constexpr int TM = 128, TN = 128, TS = 3;
 constexpr int kTCThreads = 128;
-constexpr uint32_t kTileA = TM * TK * 4;  // bytes of one 128 x 32 FP32 slice
-constexpr uint32_t kTileB = TN * TK * 4;
-constexpr uint32_t kStage = 2 * kTileA + 2 * kTileB;
-constexpr size_t kTCSmem = (size_t)TS * kStage + 1024 + 256;
-// instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9 and
-// 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
-// bits 24-28
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) |
-                            ((uint32_t)(TM >> 4) << 24);
+// Per mode: 3xTF32 (FP32 planes hi and lo of both operands, 32-wide K slabs,
+// three tf32 MMAs of K = 8 per 8 of K) or BF16 (one BF16 plane per operand,
+// 64-wide K slabs, one f16-kind MMA of K = 16 per 16 of K).  Either way a
+// slab row is 128 bytes, the span of the 128-byte swizzle.
+template <bool BF16>
+struct TcMode {
+  static constexpr int TK = BF16 ? 64 : 32;          // K elements per slab
+  static constexpr int KMMA = BF16 ? 16 : 8;         // K per MMA instruction
+  static constexpr int planes = BF16 ? 1 : 2;        // planes per operand
+  static constexpr uint32_t tileA = TM * 128;        // bytes of one plane's slab
+  static constexpr uint32_t tileB = TN * 128;
+  static constexpr uint32_t stage = planes * (tileA + tileB);
+  static constexpr size_t smem = (size_t)TS * stage + 1024 + 256;
+  // instruction descriptor: D = F32 (bits 4-5 = 1), A and B TF32 (2) or BF16
+  // (1) at bits 7-9 and 10-12, both K-major (bits 15, 16 = 0), N >> 3 at bits
+  // 17-22, M >> 4 at bits 24-28
+  static constexpr uint32_t fmt = BF16 ? 1u : 2u;
+  static constexpr uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) |
+                                    ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+};
 constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -111,7 +123,15 @@ __device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t a, uint64_t b
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      "l"(a), "l"(b), "r"(TcMode<false>::idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(TcMode<true>::idesc), "r"(acc)
       : "memory");
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
@@ -134,12 +154,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+template <bool BF16>
 __global__ void __launch_bounds__(kTCThreads, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
               const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
               int M, int N, int ktiles, int kt_per, double alpha, double beta,
               double* __restrict__ C, int ldc, double* __restrict__ part,
               unsigned int* __restrict__ status) {
+  using Md = TcMode<BF16>;
+  constexpr uint32_t kStage = Md::stage, kTileA = Md::tileA, kTileB = Md::tileB;
+  constexpr int TK = Md::TK;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -185,10 +209,15 @@ __global__ void __launch_bounds__(kTCThreads, 1)
       unsigned char* stg = base + (size_t)s * kStage;
       mbar_expect_tx(&full[s], kStage);
       const int x = (kt0 + i) * TK;
-      tma_load_2d(stg, &mAh, &full[s], x, m0);
-      tma_load_2d(stg + kTileA, &mAl, &full[s], x, m0);
-      tma_load_2d(stg + 2 * kTileA, &mBh, &full[s], x, n0);
-      tma_load_2d(stg + 2 * kTileA + kTileB, &mBl, &full[s], x, n0);
+      if constexpr (BF16) {
+        tma_load_2d(stg, &mAh, &full[s], x, m0);
+        tma_load_2d(stg + kTileA, &mBh, &full[s], x, n0);
+      } else {
+        tma_load_2d(stg, &mAh, &full[s], x, m0);
+        tma_load_2d(stg + kTileA, &mAl, &full[s], x, m0);
+        tma_load_2d(stg + 2 * kTileA, &mBh, &full[s], x, n0);
+        tma_load_2d(stg + 2 * kTileA + kTileB, &mBl, &full[s], x, n0);
+      }
       issued[s] += 1;
     }
     // no copy of this CTA may still be landing when it exits
@@ -206,15 +235,25 @@ __global__ void __launch_bounds__(kTCThreads, 1)
       }
       tc_fence_after();
       const uint32_t ah = smem_u32(base + (size_t)s * kStage);
-      const uint32_t al = ah + kTileA, bh = ah + 2 * kTileA, bl = bh + kTileB;
+      if constexpr (BF16) {
+        const uint32_t bh = ah + kTileA;
 #pragma unroll
-      for (int kk = 0; kk < TK / 8; ++kk) {
-        const uint32_t off = kk * 32;  // 8 TF32 values
-        const uint64_t dah = sdesc_sw128(ah + off), dal = sdesc_sw128(al + off);
-        const uint64_t dbh = sdesc_sw128(bh + off), dbl = sdesc_sw128(bl + off);
-        umma_tf32(tmem, dah, dbh, (i > 0 || kk > 0) ? 1u : 0u);
-        umma_tf32(tmem, dah, dbl, 1u);
-        umma_tf32(tmem, dal, dbh, 1u);
+        for (int kk = 0; kk < TK / Md::KMMA; ++kk) {
+          const uint32_t off = kk * 32;  // 16 BF16 values
+          umma_bf16(tmem, sdesc_sw128(ah + off), sdesc_sw128(bh + off),
+                    (i > 0 || kk > 0) ? 1u : 0u);
+        }
+      } else {
+        const uint32_t al = ah + kTileA, bh = ah + 2 * kTileA, bl = bh + kTileB;
+#pragma unroll
+        for (int kk = 0; kk < TK / Md::KMMA; ++kk) {
+          const uint32_t off = kk * 32;  // 8 TF32 values
+          const uint64_t dah = sdesc_sw128(ah + off), dal = sdesc_sw128(al + off);
+          const uint64_t dbh = sdesc_sw128(bh + off), dbl = sdesc_sw128(bl + off);
+          umma_tf32(tmem, dah, dbh, (i > 0 || kk > 0) ? 1u : 0u);
+          umma_tf32(tmem, dah, dbl, 1u);
+          umma_tf32(tmem, dal, dbh, 1u);
+        }
       }
       umma_commit(&empty[s]);
     }
@@ -296,6 +335,32 @@ __global__ void k_split_tf32(const double* __restrict__ X, int ldx, int rows, in
   }
 }
 
+// op(X) rounded to BF16 as a rows x kp K-contiguous array (same tiling and
+// element rule as k_split_tf32).
+__global__ void k_split_bf16(const double* __restrict__ X, int ldx, int rows, int K, int kp,
+                             int trans, __nv_bfloat16* __restrict__ out) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int j = ty; j < 32; j += 8) {
+    double v = 0.0;
+    if (trans) {
+      const int k = k0 + j, r = r0 + tx;
+      if (k < K && r < rows) v = X[(size_t)k * ldx + r];
+    } else {
+      const int r = r0 + j, k = k0 + tx;
+      if (k < K && r < rows) v = X[(size_t)r * ldx + k];
+    }
+    tile[j][tx] = v;
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int r = r0 + j, k = k0 + tx;
+    if (r < rows && k < kp)
+      out[(size_t)r * kp + k] = __float2bfloat16_rn((float)(trans ? tile[tx][j] : tile[j][tx]));
+  }
+}
+
 __global__ void k_tc_reduce(int M, int N, int nz, const double* __restrict__ part, double alpha,
                             double beta, double* __restrict__ C, int ldc) {
   const size_t mn = (size_t)M * N;
@@ -323,20 +388,23 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-int make_map(CUtensorMap* map, const float* base, int rows, int kp, int box_rows) {
+// 2-D map over a rows x kp K-contiguous plane (FP32 or BF16), box = one
+// 128-byte slab row of box_rows rows, 128-byte swizzle.
+int make_map(CUtensorMap* map, const void* base, bool bf16, int rows, int kp, int box_rows) {
   auto enc = encode_fn();
   if (!enc) {
     set_error("tensor-core GEMM: cuTensorMapEncodeTiled not available");
     return SM_ERR_CUDA;
   }
+  const size_t es = bf16 ? 2 : 4;
   const cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)kp * sizeof(float)};
-  const cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kp * es};
+  const cuuint32_t box[2] = {(cuuint32_t)(128 / es), (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
-  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims,
-                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  const CUresult r = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                         2, const_cast<void*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("tensor-core GEMM: tensor map encoding failed");
     return SM_ERR_CUDA;
@@ -354,41 +422,61 @@ bool gemm_tc_eligible(int M, int N, int K) {
 }
 
 int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
-            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc) {
+            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc,
+            bool bf16) {
+  const int TK = bf16 ? TcMode<true>::TK : TcMode<false>::TK;
   const int kp = (K + TK - 1) / TK * TK;
   const int ktiles = kp / TK;
-  float *ah, *al, *bh, *bl;
   unsigned int* status;
-  SM_CHECK(ctx.scratch("tc.Ah", (size_t)M * kp, &ah));
-  SM_CHECK(ctx.scratch("tc.Al", (size_t)M * kp, &al));
-  SM_CHECK(ctx.scratch("tc.Bh", (size_t)N * kp, &bh));
-  SM_CHECK(ctx.scratch("tc.Bl", (size_t)N * kp, &bl));
   SM_CHECK(tc_status(ctx, &status));
   // op(A)[m][k]: A[m][k] (N) or A[k][m] (T, C: real); op(B)^T[n][k]: B[k][n]
   // (N) or B[n][k] (T, C)
+  const int ta = opA == SM_OP_N ? 0 : 1, tb = opB == SM_OP_N ? 1 : 0;
   const dim3 sblk(32, 8);
-  k_split_tf32<<<dim3(kp / 32, (M + 31) / 32), sblk, 0, st>>>(A, lda, M, K, kp,
-                                                              opA == SM_OP_N ? 0 : 1, ah, al);
-  note_launch();
-  k_split_tf32<<<dim3(kp / 32, (N + 31) / 32), sblk, 0, st>>>(B, ldb, N, K, kp,
-                                                              opB == SM_OP_N ? 1 : 0, bh, bl);
-  note_launch();
-  SM_CUDA_CHECK(cudaGetLastError());
   CUtensorMap mAh, mAl, mBh, mBl;
-  SM_CHECK(make_map(&mAh, ah, M, kp, TM));
-  SM_CHECK(make_map(&mAl, al, M, kp, TM));
-  SM_CHECK(make_map(&mBh, bh, N, kp, TN));
-  SM_CHECK(make_map(&mBl, bl, N, kp, TN));
+  if (bf16) {
+    __nv_bfloat16 *ab, *bb;
+    SM_CHECK(ctx.scratch("tc.Abf", (size_t)M * kp, &ab));
+    SM_CHECK(ctx.scratch("tc.Bbf", (size_t)N * kp, &bb));
+    k_split_bf16<<<dim3(kp / 32, (M + 31) / 32), sblk, 0, st>>>(A, lda, M, K, kp, ta, ab);
+    k_split_bf16<<<dim3(kp / 32, (N + 31) / 32), sblk, 0, st>>>(B, ldb, N, K, kp, tb, bb);
+    note_launch(2);
+    SM_CUDA_CHECK(cudaGetLastError());
+    SM_CHECK(make_map(&mAh, ab, true, M, kp, TM));
+    SM_CHECK(make_map(&mBh, bb, true, N, kp, TN));
+    mAl = mAh;
+    mBl = mBh;
+  } else {
+    float *ah, *al, *bh, *bl;
+    SM_CHECK(ctx.scratch("tc.Ah", (size_t)M * kp, &ah));
+    SM_CHECK(ctx.scratch("tc.Al", (size_t)M * kp, &al));
+    SM_CHECK(ctx.scratch("tc.Bh", (size_t)N * kp, &bh));
+    SM_CHECK(ctx.scratch("tc.Bl", (size_t)N * kp, &bl));
+    k_split_tf32<<<dim3(kp / 32, (M + 31) / 32), sblk, 0, st>>>(A, lda, M, K, kp, ta, ah, al);
+    k_split_tf32<<<dim3(kp / 32, (N + 31) / 32), sblk, 0, st>>>(B, ldb, N, K, kp, tb, bh, bl);
+    note_launch(2);
+    SM_CUDA_CHECK(cudaGetLastError());
+    SM_CHECK(make_map(&mAh, ah, false, M, kp, TM));
+    SM_CHECK(make_map(&mAl, al, false, M, kp, TM));
+    SM_CHECK(make_map(&mBh, bh, false, N, kp, TN));
+    SM_CHECK(make_map(&mBl, bl, false, N, kp, TN));
+  }
   const int tiles = ((M + TM - 1) / TM) * ((N + TN - 1) / TN);
   int nz = std::max(1, std::min(std::max(1, ctx.num_sms) / tiles, ktiles / 2));
   const int kt_per = (ktiles + nz - 1) / nz;
   nz = (ktiles + kt_per - 1) / kt_per;
   double* part = nullptr;
   if (nz > 1) SM_CHECK(ctx.scratch("tc.part", (size_t)nz * M * N, &part));
-  SM_CHECK(raise_smem_limit(k_gemm_tc, kTCSmem));
   const dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, nz);
-  k_gemm_tc<<<grid, kTCThreads, kTCSmem, st>>>(mAh, mAl, mBh, mBl, M, N, ktiles, kt_per, alpha,
-                                               beta, C, ldc, part, status);
+  if (bf16) {
+    SM_CHECK(raise_smem_limit(k_gemm_tc<true>, TcMode<true>::smem));
+    k_gemm_tc<true><<<grid, kTCThreads, TcMode<true>::smem, st>>>(
+        mAh, mAl, mBh, mBl, M, N, ktiles, kt_per, alpha, beta, C, ldc, part, status);
+  } else {
+    SM_CHECK(raise_smem_limit(k_gemm_tc<false>, TcMode<false>::smem));
+    k_gemm_tc<false><<<grid, kTCThreads, TcMode<false>::smem, st>>>(
+        mAh, mAl, mBh, mBl, M, N, ktiles, kt_per, alpha, beta, C, ldc, part, status);
+  }
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   if (nz > 1) {

@@ -134,8 +134,10 @@ int gemm_ctx_f32(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int 
 // out set bits of a device status word; tc_status_check reads (and clears) it
 // and returns SM_ERR_CUDA when one did.
 bool gemm_tc_eligible(int M, int N, int K);
+// bf16 = true: one BF16 product (kind::f16, FP32 accumulation) instead of 3xTF32
 int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
-            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc);
+            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc,
+            bool bf16 = false);
 int tc_status(Ctx& ctx, unsigned int** out);
 int tc_status_check(Ctx& ctx, cudaStream_t st);
 
@@ -146,6 +148,11 @@ int tc_status_check(Ctx& ctx, cudaStream_t st);
 bool gemm_oz_eligible(int M, int N, int K);
 int gemm_oz(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
             const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc);
+
+// --- dmrg.cu -----------------------------------------------------------------
+template <typename T>
+int two_site_matvec(Ctx& ctx, cudaStream_t st, int a, int c, int b, int p1, int p2, int e, int g,
+                    int f, const T* L, const T* H, const T* R, const T* v, T* out, int precision);
 
 // --- mps_ops.cu ------------------------------------------------------------
 template <typename T>
