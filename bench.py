@@ -211,6 +211,7 @@ def workload_config(args):
                         f"+ variational simplify, tol 1e-12, max bond {args.chi}, 2 sweeps",
             "n": args.n, "chi": args.chi, "mpo_bond": 3, "tolerance": 1e-12,
             "max_bond_dimension": args.chi, "sweeps_per_step": 2, "form": args.form,
+            "rank_cap": [getattr(args, "cap_margin", 1.15), getattr(args, "cap_extra", 10)],
             "contractions": getattr(args, "contractions", "fp32"),
             "l2": "flushed between timed steps (256 MB write); the product MPS is >256 MB",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
@@ -472,6 +473,9 @@ def main():
     ap.add_argument("--train-count", type=int, default=90,
                     help="training workloads recorded when the predictor is trained here")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cap-margin", type=float, default=1.15,
+                    help="learned cap of the FP32 QR: ceil(margin * predicted rank) + extra rows")
+    ap.add_argument("--cap-extra", type=int, default=10)
     ap.add_argument("--split-case", type=int, nargs=2, metavar=("M", "N"),
                     help="time single M x N two-site splits in both precision modes and exit")
     ap.add_argument("--gemm-case", type=int, nargs=3, metavar=("M", "N", "K"),
@@ -575,6 +579,7 @@ def main():
                  "ms_per_step": sum(pt) / len(pt)}
     sg.set_precision({"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed+learned"}[args.form],
                      contractions=args.contractions)
+    _lib.check(_lib.load().sm_ctx_set_rank_cap(_lib.context(), args.cap_margin, args.cap_extra))
 
     for _ in range(max(3, args.warmup)):
         out = step()
@@ -734,6 +739,8 @@ def main():
                 "cluster_jacobi_ms_per_step": timed_stats["cluster_jacobi_ms"] / k,
                 "fallbacks_coupling_per_step": timed_stats["mixed_fallback_cut"] / k,
                 "fallbacks_fp32_per_step": timed_stats["mixed_fallback_fp32"] / k,
+                "fallbacks_over_tolerance_per_step": timed_stats["mixed_fallback_over"] / k,
+                "fallbacks_unconverged_per_step": timed_stats["mixed_fallback_unconverged"] / k,
                 "capped_per_step": timed_stats["mixed_capped"] / k,
                 "cap_redone_per_step": timed_stats["mixed_cap_redone"] / k,
                 "mean_predicted_rank": timed_stats["rank_predicted_sum"]

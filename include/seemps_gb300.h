@@ -108,6 +108,9 @@ enum { SM_PRECISION_FP64 = 0, SM_PRECISION_MIXED = 1, SM_PRECISION_MIXED_LEARNED
  * without the cap, and the exact discarded-weight check still sends tolerance
  * violations to the FP64 Jacobi SVD. */
 int sm_ctx_set_precision(void* ctx, int precision);
+/* SM_PRECISION_MIXED_LEARNED's cap on the FP32 QR: ceil(margin * r) + extra
+ * rows for a predicted rank r (default 1.15 and 10; margin >= 1, extra >= 0). */
+int sm_ctx_set_rank_cap(void* ctx, double margin, int extra);
 /* Arithmetic of the sweep contractions (environments, two-site tensors,
  * canonical absorptions) in the mixed forms: 64 (default, FP64) or 32 (FP32
  * arithmetic on FP64 data, ~1e-7 relative error per contraction).  Ignored in
@@ -370,6 +373,8 @@ typedef struct sm_stats {
   int64_t gemm_tc_launches;    /* of those, on the tensor cores (3xTF32, tcgen05) */
   double gemm_tc_flops;        /* 2 M N K of those (the MMAs run 3x this) */
   double gemm_tc_ms;           /* event-timed (stats timing on), split + MMA + reduce */
+  int64_t mixed_fallback_over; /* of the FP32 fallbacks: exact discarded weight over tolerance */
+  int64_t mixed_fallback_unconverged; /* of the FP32 fallbacks: FP32 iteration did not converge */
   int64_t gemm_oz_launches;    /* FP64 products on the BF16 tensor cores (mixed forms) */
   double gemm_oz_flops;        /* 2 M N K of those */
   double gemm_oz_ms;           /* event-timed (stats timing on), slicing + MMA + reduce */

@@ -77,6 +77,8 @@ class sm_stats(C.Structure):
         ("gemm_tc_launches", C.c_int64),
         ("gemm_tc_flops", C.c_double),
         ("gemm_tc_ms", C.c_double),
+        ("mixed_fallback_over", C.c_int64),
+        ("mixed_fallback_unconverged", C.c_int64),
         ("gemm_oz_launches", C.c_int64),
         ("gemm_oz_flops", C.c_double),
         ("gemm_oz_ms", C.c_double),
@@ -110,6 +112,7 @@ SIGNATURES = {
                                 C.c_int, vp, C.c_int, vp, C.c_int, vp]),
     "sm_ctx_set_fp64_products": (C.c_int, [vp, C.c_int]),
     "sm_ctx_set_concurrent": (C.c_int, [vp, C.c_int]),
+    "sm_ctx_set_rank_cap": (C.c_int, [vp, C.c_double, C.c_int]),
     "sm_two_site_matvec": (C.c_int, [vp, C.c_int, ip, vp, vp, vp, vp, vp, C.c_int, vp]),
     "sm_svd": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp]),
     "sm_left_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,

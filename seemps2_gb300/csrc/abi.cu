@@ -370,6 +370,17 @@ int sm_two_site_matvec(void* ctx, int dtype, const int* dims, const void* L, con
   return precision == SM_MATVEC_FP64 ? SM_OK : tc_status_check(c, s);
 }
 
+int sm_ctx_set_rank_cap(void* ctx, double margin, int extra) {
+  SM_GUARD_CTX(ctx);
+  if (!(margin >= 1.0) || extra < 0) {
+    set_error("sm_ctx_set_rank_cap: margin must be >= 1 and extra >= 0");
+    return SM_ERR_VALUE;
+  }
+  as_ctx(ctx)->cap_margin = margin;
+  as_ctx(ctx)->cap_extra = extra;
+  return SM_OK;
+}
+
 int sm_ctx_set_concurrent(void* ctx, int on) {
   SM_GUARD_CTX(ctx);
   as_ctx(ctx)->concurrent = on != 0;

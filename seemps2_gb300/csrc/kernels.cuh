@@ -34,6 +34,9 @@ struct Ctx {
   bool contract32 = false;  // mixed forms: sweep contractions in FP32 arithmetic
   bool fp64_tc = true;      // mixed forms: FP64 products on the tensor cores (gemm_oz)
   bool concurrent = false;  // shares the device with other streams: no multi-CTA grid barriers
+  // learned rank cap of the FP32 QR: ceil(cap_margin * predicted) + cap_extra rows
+  double cap_margin = 1.15;
+  int cap_extra = 10;
   int split_site = -1, split_n = 0;
   int prev_rank = 0;
   std::vector<double> prev_s;

@@ -1113,8 +1113,6 @@ constexpr int kMixedRefine = 2;    // refinement steps
 constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
 constexpr double kMixedCutAmp = 1e-6;  // largest kept/dropped coupling (angle s_i / |A|)
 constexpr double kMixedMinTol = 1e-14;   // smallest relative-norm tolerance taken in mixed
-constexpr int kCapOversample = 10;    // QR rows beyond the predicted rank
-constexpr double kCapMargin = 1.15;   // relative margin on the predicted rank
 
 template <typename T>
 __global__ void k_gather_rows(const T* __restrict__ rows, int l, const int* __restrict__ perm,
@@ -1435,6 +1433,12 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   else if (strat.method == SM_RELATIVE_SINGULAR_VALUE)
     thr_rel = std::min(1e-10, 1e-2 * strat.tolerance * strat.tolerance);
   else thr_abs = 1e-2 * strat.tolerance * strat.tolerance;
+  // The FP32 trailing-weight estimate is rounding noise below ~1e-7 |W|^2, so
+  // a QR that stops on it can leave weight that the exact FP64 check finds
+  // over the tolerance (the tolerance-limited splits of the n=30 chi=256
+  // workload at tol 1e-12 did).  The redo of such a split (qr_cap = min(m, n))
+  // therefore runs the full QR.
+  if (qr_cap >= std::min(m, n)) thr_rel = thr_abs = 0.0;
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
   // a predicted rank caps the rank-revealing QR (qr_cap rows of R)
@@ -1472,6 +1476,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   if (hc.status != 0 || (!exact_rule && h->info[3] < kMixedBlind * h->info[2])) {
     ctx.stats.mixed_fallbacks += 1;
     ctx.stats.mixed_fallback_fp32 += 1;
+    if (hc.status != 0) ctx.stats.mixed_fallback_unconverged += 1;
     return SM_OK;
   }
   const int cnt = std::max(1, std::min(hc.nact, k));
@@ -1552,12 +1557,14 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // a capped QR that left weight the rank may need: more than 1% of what the
   // tolerance allows (and more than 1e-12 of |A|^2) outside the rows' span,
   // computed exactly after the refinement
-  const bool missed = qr_cap > 0 && hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
+  const bool missed = qr_cap > 0 && qr_cap < k &&
+                      hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
   const bool coupled = !(cut_angle <= kMixedCutAmp);
   const bool over = D < strat.max_bond_dimension && D < k &&
                     r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
-  if (missed && !blind && !coupled) {
-    // the cap was too small: the caller retries with the uncapped QR
+  if ((missed || (over && qr_cap > 0 && qr_cap < k)) && !blind && !coupled) {
+    // the cap (or the QR's stop) left weight the rank needs: the caller
+    // retries with the full QR
     ctx.stats.mixed_cap_redone += 1;
     *missed_out = true;
     return SM_OK;
@@ -1566,6 +1573,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     ctx.stats.mixed_fallbacks += 1;
     if (coupled) ctx.stats.mixed_fallback_cut += 1;
     else ctx.stats.mixed_fallback_fp32 += 1;
+    if (over && !coupled && !blind) ctx.stats.mixed_fallback_over += 1;
     return SM_OK;
   }
   T* iso = want_u ? left : right;
@@ -1611,16 +1619,16 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
         strat.tolerance >= kMixedMinTol) {
       int r = 0;
       SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
-      cap = std::min(std::min(m, n), (int)std::ceil(kCapMargin * r) + kCapOversample);
+      cap = std::min(std::min(m, n), (int)std::ceil(ctx.cap_margin * r) + ctx.cap_extra);
       ctx.stats.rank_predicted_sum += r;
     }
     bool done = false, missed = false;
     SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, cap,
                                 &missed));
     if (done) return SM_OK;
-    if (missed)  // predicted rank too small: the QR without the cap
-      SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, 0,
-                                  &missed));
+    if (missed)  // predicted rank too small: the full QR
+      SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done,
+                                  std::min(m, n), &missed));
     if (done) return SM_OK;
   }
   if (xu) return svd_split_xfree<T>(ctx, st, A, m, n, strat, true, left, right, s_out, out);
