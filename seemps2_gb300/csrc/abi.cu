@@ -242,15 +242,17 @@ int sm_split_rows_f32(void* ctx, int dtype, const void* A, int m, int n, int wan
   }
   JacobiCtl* ctl;
   double* info;
+  float* vbuf;
   SM_CHECK(c.scratch("rows.ctl", 1, &ctl));
-  SM_CHECK(c.scratch("rows.info", 4, &info));
+  SM_CHECK(c.scratch("rows.info", 8, &info));
+  SM_CHECK(c.scratch("rows.vbuf", split_cluster_vbuf_floats(kw), &vbuf));
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
   if (dtype == SM_FLOAT64)
     SM_CHECK(split_cluster_f32<double>(st, (const double*)A, m, n, want_u != 0, thr_rel, thr_abs,
-                                       60, (double*)rows, nrm, kcap, ctl, info));
+                                       60, (double*)rows, nrm, kcap, ctl, info, 0, vbuf));
   else
     SM_CHECK(split_cluster_f32<cplx>(st, (const cplx*)A, m, n, want_u != 0, thr_rel, thr_abs, 60,
-                                     (cplx*)rows, nrm, kcap, ctl, info));
+                                     (cplx*)rows, nrm, kcap, ctl, info, 0, vbuf));
   JacobiCtl* h = reinterpret_cast<JacobiCtl*>(c.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(h, ctl, sizeof(JacobiCtl), cudaMemcpyDeviceToHost, st));
   SM_CUDA_CHECK(cudaStreamSynchronize(st));

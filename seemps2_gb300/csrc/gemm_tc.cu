@@ -154,12 +154,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-template <bool BF16>
+template <bool BF16, typename OutT>
 __global__ void __launch_bounds__(kTCThreads, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
               const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
               int M, int N, int ktiles, int kt_per, double alpha, double beta,
-              double* __restrict__ C, int ldc, double* __restrict__ part,
+              OutT* __restrict__ C, int ldc, OutT* __restrict__ part,
               unsigned int* __restrict__ status) {
   using Md = TcMode<BF16>;
   constexpr uint32_t kStage = Md::stage, kTileA = Md::tileA, kTileB = Md::tileB;
@@ -275,10 +275,11 @@ __global__ void __launch_bounds__(kTCThreads, 1)
           const int col = n0 + c + j;
           if (col < N) {
             if (part) {
-              part[((size_t)blockIdx.z * M + row) * N + col] = (double)v[j];
+              part[((size_t)blockIdx.z * M + row) * N + col] = (OutT)v[j];
             } else {
-              double* p = C + (size_t)row * ldc + col;
-              *p = beta == 0.0 ? alpha * (double)v[j] : fma(alpha, (double)v[j], beta * *p);
+              OutT* p = C + (size_t)row * ldc + col;
+              *p = beta == 0.0 ? (OutT)(alpha * (double)v[j])
+                               : (OutT)fma(alpha, (double)v[j], beta * (double)*p);
             }
           }
         }
@@ -361,15 +362,16 @@ __global__ void k_split_bf16(const double* __restrict__ X, int ldx, int rows, in
   }
 }
 
-__global__ void k_tc_reduce(int M, int N, int nz, const double* __restrict__ part, double alpha,
-                            double beta, double* __restrict__ C, int ldc) {
+template <typename OutT>
+__global__ void k_tc_reduce(int M, int N, int nz, const OutT* __restrict__ part, double alpha,
+                            double beta, OutT* __restrict__ C, int ldc) {
   const size_t mn = (size_t)M * N;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < mn;
        e += (size_t)gridDim.x * blockDim.x) {
     double acc = 0.0;
-    for (int z = 0; z < nz; ++z) acc += part[(size_t)z * mn + e];
-    double* p = C + (e / N) * ldc + (e % N);
-    *p = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *p);
+    for (int z = 0; z < nz; ++z) acc += (double)part[(size_t)z * mn + e];
+    OutT* p = C + (e / N) * ldc + (e % N);
+    *p = beta == 0.0 ? (OutT)(alpha * acc) : (OutT)fma(alpha, acc, beta * (double)*p);
   }
 }
 
@@ -421,72 +423,95 @@ bool gemm_tc_eligible(int M, int N, int K) {
          encode_fn() != nullptr;
 }
 
-int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
-            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc,
-            bool bf16) {
-  const int TK = bf16 ? TcMode<true>::TK : TcMode<false>::TK;
-  const int kp = (K + TK - 1) / TK * TK;
+int tc_kslab(bool bf16) { return bf16 ? TcMode<true>::TK : TcMode<false>::TK; }
+
+int tc_planes(Ctx& ctx, cudaStream_t st, const double* X, int ldx, int rows, int K, int kp,
+              int trans, bool bf16, void* hi, float* lo) {
+  const dim3 sblk(32, 8), grd(kp / 32, (rows + 31) / 32);
+  if (bf16)
+    k_split_bf16<<<grd, sblk, 0, st>>>(X, ldx, rows, K, kp, trans,
+                                       reinterpret_cast<__nv_bfloat16*>(hi));
+  else
+    k_split_tf32<<<grd, sblk, 0, st>>>(X, ldx, rows, K, kp, trans, reinterpret_cast<float*>(hi),
+                                       lo);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
+}
+
+template <typename OutT>
+int gemm_tc_planes(Ctx& ctx, cudaStream_t st, int M, int N, int kp, bool bf16, const void* ah,
+                   const float* al, const void* bh, const float* bl, double alpha, double beta,
+                   OutT* C, int ldc) {
+  const int TK = tc_kslab(bf16);
   const int ktiles = kp / TK;
   unsigned int* status;
   SM_CHECK(tc_status(ctx, &status));
-  // op(A)[m][k]: A[m][k] (N) or A[k][m] (T, C: real); op(B)^T[n][k]: B[k][n]
-  // (N) or B[n][k] (T, C)
-  const int ta = opA == SM_OP_N ? 0 : 1, tb = opB == SM_OP_N ? 1 : 0;
-  const dim3 sblk(32, 8);
   CUtensorMap mAh, mAl, mBh, mBl;
+  SM_CHECK(make_map(&mAh, ah, bf16, M, kp, TM));
+  SM_CHECK(make_map(&mBh, bh, bf16, N, kp, TN));
   if (bf16) {
-    __nv_bfloat16 *ab, *bb;
-    SM_CHECK(ctx.scratch("tc.Abf", (size_t)M * kp, &ab));
-    SM_CHECK(ctx.scratch("tc.Bbf", (size_t)N * kp, &bb));
-    k_split_bf16<<<dim3(kp / 32, (M + 31) / 32), sblk, 0, st>>>(A, lda, M, K, kp, ta, ab);
-    k_split_bf16<<<dim3(kp / 32, (N + 31) / 32), sblk, 0, st>>>(B, ldb, N, K, kp, tb, bb);
-    note_launch(2);
-    SM_CUDA_CHECK(cudaGetLastError());
-    SM_CHECK(make_map(&mAh, ab, true, M, kp, TM));
-    SM_CHECK(make_map(&mBh, bb, true, N, kp, TN));
     mAl = mAh;
     mBl = mBh;
   } else {
-    float *ah, *al, *bh, *bl;
-    SM_CHECK(ctx.scratch("tc.Ah", (size_t)M * kp, &ah));
-    SM_CHECK(ctx.scratch("tc.Al", (size_t)M * kp, &al));
-    SM_CHECK(ctx.scratch("tc.Bh", (size_t)N * kp, &bh));
-    SM_CHECK(ctx.scratch("tc.Bl", (size_t)N * kp, &bl));
-    k_split_tf32<<<dim3(kp / 32, (M + 31) / 32), sblk, 0, st>>>(A, lda, M, K, kp, ta, ah, al);
-    k_split_tf32<<<dim3(kp / 32, (N + 31) / 32), sblk, 0, st>>>(B, ldb, N, K, kp, tb, bh, bl);
-    note_launch(2);
-    SM_CUDA_CHECK(cudaGetLastError());
-    SM_CHECK(make_map(&mAh, ah, false, M, kp, TM));
     SM_CHECK(make_map(&mAl, al, false, M, kp, TM));
-    SM_CHECK(make_map(&mBh, bh, false, N, kp, TN));
     SM_CHECK(make_map(&mBl, bl, false, N, kp, TN));
   }
   const int tiles = ((M + TM - 1) / TM) * ((N + TN - 1) / TN);
   int nz = std::max(1, std::min(std::max(1, ctx.num_sms) / tiles, ktiles / 2));
   const int kt_per = (ktiles + nz - 1) / nz;
   nz = (ktiles + kt_per - 1) / kt_per;
-  double* part = nullptr;
-  if (nz > 1) SM_CHECK(ctx.scratch("tc.part", (size_t)nz * M * N, &part));
+  OutT* part = nullptr;
+  if (nz > 1) SM_CHECK(ctx.scratch(sizeof(OutT) == 8 ? "tc.part" : "tc.part32", (size_t)nz * M * N, &part));
   const dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, nz);
   if (bf16) {
-    SM_CHECK(raise_smem_limit(k_gemm_tc<true>, TcMode<true>::smem));
-    k_gemm_tc<true><<<grid, kTCThreads, TcMode<true>::smem, st>>>(
+    SM_CHECK(raise_smem_limit(k_gemm_tc<true, OutT>, TcMode<true>::smem));
+    k_gemm_tc<true, OutT><<<grid, kTCThreads, TcMode<true>::smem, st>>>(
         mAh, mAl, mBh, mBl, M, N, ktiles, kt_per, alpha, beta, C, ldc, part, status);
   } else {
-    SM_CHECK(raise_smem_limit(k_gemm_tc<false>, TcMode<false>::smem));
-    k_gemm_tc<false><<<grid, kTCThreads, TcMode<false>::smem, st>>>(
+    SM_CHECK(raise_smem_limit(k_gemm_tc<false, OutT>, TcMode<false>::smem));
+    k_gemm_tc<false, OutT><<<grid, kTCThreads, TcMode<false>::smem, st>>>(
         mAh, mAl, mBh, mBl, M, N, ktiles, kt_per, alpha, beta, C, ldc, part, status);
   }
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   if (nz > 1) {
     const size_t mn = (size_t)M * N;
-    k_tc_reduce<<<(int)std::min<size_t>((mn + 255) / 256, 4096), 256, 0, st>>>(M, N, nz, part,
-                                                                               alpha, beta, C, ldc);
+    k_tc_reduce<OutT><<<(int)std::min<size_t>((mn + 255) / 256, 4096), 256, 0, st>>>(
+        M, N, nz, part, alpha, beta, C, ldc);
     note_launch();
     SM_CUDA_CHECK(cudaGetLastError());
   }
   return SM_OK;
+}
+
+template int gemm_tc_planes<double>(Ctx&, cudaStream_t, int, int, int, bool, const void*,
+                                    const float*, const void*, const float*, double, double,
+                                    double*, int);
+template int gemm_tc_planes<float>(Ctx&, cudaStream_t, int, int, int, bool, const void*,
+                                   const float*, const void*, const float*, double, double, float*,
+                                   int);
+
+int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
+            const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc,
+            bool bf16) {
+  const int TK = tc_kslab(bf16);
+  const int kp = (K + TK - 1) / TK * TK;
+  // op(A)[m][k]: A[m][k] (N) or A[k][m] (T, C: real); op(B)^T[n][k]: B[k][n]
+  // (N) or B[n][k] (T, C)
+  const int ta = opA == SM_OP_N ? 0 : 1, tb = opB == SM_OP_N ? 1 : 0;
+  void *ah, *bh;
+  float *al = nullptr, *bl = nullptr;
+  const size_t es = bf16 ? 2 : 4;
+  SM_CHECK(ctx.scratch(bf16 ? "tc.Abf" : "tc.Ah", es * (size_t)M * kp, &ah));
+  SM_CHECK(ctx.scratch(bf16 ? "tc.Bbf" : "tc.Bh", es * (size_t)N * kp, &bh));
+  if (!bf16) {
+    SM_CHECK(ctx.scratch("tc.Al", (size_t)M * kp, &al));
+    SM_CHECK(ctx.scratch("tc.Bl", (size_t)N * kp, &bl));
+  }
+  SM_CHECK(tc_planes(ctx, st, A, lda, M, K, kp, ta, bf16, ah, al));
+  SM_CHECK(tc_planes(ctx, st, B, ldb, N, K, kp, tb, bf16, bh, bl));
+  return gemm_tc_planes<double>(ctx, st, M, N, kp, bf16, ah, al, bh, bl, alpha, beta, C, ldc);
 }
 
 int tc_status(Ctx& ctx, unsigned int** out) {

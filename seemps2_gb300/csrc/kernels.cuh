@@ -141,6 +141,18 @@ bool gemm_tc_eligible(int M, int N, int K);
 int gemm_tc(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
             const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc,
             bool bf16 = false);
+// Operands already in tensor-core form: K-contiguous planes of M x kp and
+// N x kp (kp a multiple of tc_kslab(bf16)): one BF16 plane, or FP32 hi and lo
+// planes for 3xTF32.  tc_planes writes them from an FP64 op(X) (trans as in
+// gemm_tc's operand rule); gemm_tc_planes multiplies them, C (double or float)
+// = alpha A_planes B_planes^T + beta C.
+int tc_kslab(bool bf16);
+int tc_planes(Ctx& ctx, cudaStream_t st, const double* X, int ldx, int rows, int K, int kp,
+              int trans, bool bf16, void* hi, float* lo);
+template <typename OutT>
+int gemm_tc_planes(Ctx& ctx, cudaStream_t st, int M, int N, int kp, bool bf16, const void* ah,
+                   const float* al, const void* bh, const float* bl, double alpha, double beta,
+                   OutT* C, int ldc);
 int tc_status(Ctx& ctx, unsigned int** out);
 int tc_status_check(Ctx& ctx, cudaStream_t st);
 
@@ -211,10 +223,12 @@ bool split_cluster_fits(int kw, int l);
 // info[0] = |A|_F^2 (FP64), info[1] = trailing weight dropped by the QR.
 // qr_cap > 0 stops the QR after that many steps (a predicted rank) even if
 // the trailing weight is still above the threshold; info[1] then holds the
-// weight it left behind.
+// weight it left behind.  info needs 7 doubles; vbuf (device) needs
+// split_cluster_vbuf_floats(kw) floats, kw = n when U is wanted, else m.
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, int qr_cap = 0);
+                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf);
+size_t split_cluster_vbuf_floats(int kw);
 
 }  // namespace sm

@@ -1425,6 +1425,8 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(ctx.scratch("mx.perm", (size_t)kcap, &perm));
   SM_CHECK(ctx.scratch("mx.info", 8, &info));
   SM_CHECK(ctx.scratch("mx.ctl", 1, &ctl));
+  float* vbuf;
+  SM_CHECK(ctx.scratch("mx.vbuf", split_cluster_vbuf_floats(want_u ? n : m), &vbuf));
   SM_CHECK(ctx.scratch("mx.res", 1, &res));
   // RRQR stop: drop at most 1% of what the tolerance allows (never more than
   // 1e-10 of |A|^2, which the power step then suppresses further)
@@ -1444,7 +1446,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // a predicted rank caps the rank-revealing QR (qr_cap rows of R)
   if (qr_cap > 0) ctx.stats.mixed_capped += 1;
   SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
-                                info, qr_cap));
+                                info, qr_cap, vbuf));
   if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
   struct Head {
     JacobiCtl c;

@@ -11,13 +11,24 @@
 //   phase 0  |W|_F^2 in FP64; W / |W|_F is stored in FP32, column c of W in
 //            the shared memory of CTA c % 16 (so FP32 cannot overflow even
 //            for operators with 1/h^2 ~ 1e18 entries).
-//   phase 1  Householder QR of W (reflectors act on the columns, length kw),
-//            one cluster barrier per step; the warp that owns column j + 1
-//            forms the next reflector in the same step and its CTA pushes it
-//            into every other CTA before the barrier (no read after the
-//            barrier leaves the SM).  The factorisation stops once the
-//            trailing block holds at most thr of |W|_F^2 (rank revealing),
-//            leaving keff rows of R.
+//   phase 1  blocked Householder QR of W (reflectors act on the columns,
+//            length kw).  The columns are dealt out in blocks of qb (<= 8):
+//            block g lives in CTA g % 16.  One cluster barrier per block
+//            step: every CTA applies the block's qb reflectors to its columns
+//            beyond it in compact WY form (two passes over the rows; lanes
+//            own columns and warps own rows, so every reflector-row load is a
+//            shared-memory broadcast), then the CTA owning the next block
+//            factors that block's columns (its "panel": qb reflectors, one
+//            named barrier of the panel warps each) and writes the reflector
+//            block and its T factor once to global memory; after the barrier
+//            every other CTA copies them from L2 into its shared memory (a
+//            DSMEM broadcast from one SM to 15 is bound by that SM's outgoing
+//            stores, ~5 bytes per clock).  The
+//            factorisation stops at the first step whose trailing block holds
+//            at most thr of |W|_F^2 (rank revealing), leaving keff rows of R;
+//            the trailing weights of all qb steps of a block come from the
+//            column weights after the block (the later reflectors of a block
+//            leave the weight below each earlier step unchanged).
 //   phase 2  the rows of R are cut into 32 blocks of r = ceil(keff / 32) rows;
 //            CTA c holds block positions c and 31 - c in shared memory.
 //   phase 3  block-cyclic one-sided Jacobi: per sweep, the pairs inside each
@@ -52,6 +63,31 @@ constexpr int kCW = 16;            // CTAs per cluster
 constexpr int kCNT = 512;          // threads per CTA
 constexpr int kCNW = kCNT / 32;    // warps per CTA
 constexpr int kMaxRows = 512;      // rows of R the Jacobi phase takes (32 blocks of <= 16)
+constexpr int kQB = 8;             // widest column block of the QR (reflectors per cluster barrier)
+constexpr int kPanelRP = 2;        // rows per thread of the QR panel in registers (kw <= 1024)
+
+// column slots per CTA for l columns in blocks of qb
+__host__ __device__ inline int qr_slots(int l, int qb) {
+  return ((l + qb * kCW - 1) / (qb * kCW)) * qb;
+}
+// Shared memory of the QR phase: the columns [ncs][ks] (ks = kw | 1: an odd
+// stride keeps lanes that own different columns on different banks; padded
+// to 16 bytes), two reflector blocks [kwp][qb] (kwp = kw rounded up to a
+// multiple of 4, so each block is a multiple of 16 bytes), two T factors
+// [8][8], and the block update's scratch:
+// y partials [16][qb][32] and sums [qb][32] (F), row weights [qb][32] and
+// tail weights [16][32] (float).
+template <typename F>
+__host__ __device__ inline size_t qr_cols_elems(int ncs, int kw) {
+  const size_t per16 = 16 / sizeof(F);
+  return ((size_t)ncs * (kw | 1) + per16 - 1) / per16 * per16;
+}
+template <typename F>
+__host__ __device__ inline size_t qr_bytes(int ncs, int kw, int qb) {
+  const size_t kwp = (size_t)((kw + 3) & ~3);
+  const size_t slab = sizeof(F) * (size_t)(kCNW + 1) * qb * 32 + sizeof(float) * (size_t)(qb + kCNW) * 32;
+  return sizeof(F) * (qr_cols_elems<F>(ncs, kw) + 2 * kwp * qb + 2 * kQB * kQB) + slab;
+}
 
 // ---- FP32 element helpers ----------------------------------------------------
 template <typename T> struct F32;
@@ -91,20 +127,23 @@ __device__ __forceinline__ float f_im(float2 x) { return x.y; }
 __device__ __forceinline__ void f_set(float& x, float re, float) { x = re; }
 __device__ __forceinline__ void f_set(float2& x, float re, float im) { x = make_float2(re, im); }
 
-// Rotation of a row pair: p' = c p - s conj(e) q ; q' = s e p + c q, with e
-// the phase of g = <p, q>.
-__device__ __forceinline__ void f_rot(float& p, float& q, float c, float s, float er, float) {
-  const float np = fmaf(c, p, -s * er * q);
-  const float nq = fmaf(s * er, p, c * q);
-  p = np;
-  q = nq;
+__device__ __forceinline__ float shfl_f(float x, int src) {
+  return __shfl_sync(0xffffffffu, x, src);
 }
-__device__ __forceinline__ void f_rot(float2& p, float2& q, float c, float s, float er, float ei) {
-  const float ar = s * er, ai = s * ei;
-  const float2 np = make_float2(c * p.x - (ar * q.x + ai * q.y), c * p.y - (ar * q.y - ai * q.x));
-  const float2 nq = make_float2((ar * p.x - ai * p.y) + c * q.x, (ar * p.y + ai * p.x) + c * q.y);
-  p = np;
-  q = nq;
+__device__ __forceinline__ float2 shfl_f(float2 x, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, x.x, src), __shfl_sync(0xffffffffu, x.y, src));
+}
+
+// the elements of a float4 as F values
+__device__ __forceinline__ void unpack4(float4 t, float* v) {
+  v[0] = t.x;
+  v[1] = t.y;
+  v[2] = t.z;
+  v[3] = t.w;
+}
+__device__ __forceinline__ void unpack4(float4 t, float2* v) {
+  v[0] = make_float2(t.x, t.y);
+  v[1] = make_float2(t.z, t.w);
 }
 
 __device__ __forceinline__ float warp_sum(float x) {
@@ -120,13 +159,41 @@ __device__ __forceinline__ double warp_sum(double x) {
 
 // Control words of one CTA (after the data region of its shared memory).
 struct CtrlS {
-  int flag[2];        // CTA 0: a rotation happened in the sweep of this parity
-  float tau[2];       // reflector tau, by step parity (pushed by the owner)
-  float part[2][kCW]; // trailing-weight partials of all CTAs, by step parity
-  double part64[kCW]; // |W|^2 partials of all CTAs
-  float red[kCNW];    // CTA-local reduction scratch
+  int flag[2];                 // CTA 0: a rotation happened in the sweep of this parity
+  float2 gram[kQB][kQB];       // panel reflector Gram matrix v_i^H v_k (i < k; re, im)
+  float2 prow[kQB];            // the panel's pivot row (re, im), while it is factored
+  float rsq[kQB][kQB];         // |R|^2 of the rows just below the panel's first row
+  float pred[kCNW][16];        // CTA-sum partials
+  float pfin[16];
+  float part[2][kCW][kQB];     // trailing-weight partials of all CTAs, by block-step parity
+  float inpanel[kQB][kQB];     // owner of a panel: weight of panel column k below step i
+  double part64[kCW];          // |W|^2 partials of all CTAs
+  float red[kCNW][kQB];        // CTA-local reduction scratch
   double red64[kCNW];
 };
+
+// CTA-wide sum of n <= 16 floats (every thread gets the sums; fixed order).
+__device__ __forceinline__ void cta_sum(CtrlS* ctrl, float (&v)[16], int n) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int a = 0; a < 16; ++a)
+    if (a < n) v[a] = warp_sum(v[a]);
+  if (lane == 0) {
+#pragma unroll
+    for (int a = 0; a < 16; ++a)
+      if (a < n) ctrl->pred[warp][a] = v[a];
+  }
+  __syncthreads();
+  if (tid < n) {
+    float t = 0.f;
+    for (int w = 0; w < kCNW; ++w) t += ctrl->pred[w][tid];
+    ctrl->pfin[tid] = t;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < 16; ++a)
+    if (a < n) v[a] = ctrl->pfin[a];
+}
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -136,10 +203,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // Shared memory (bytes) for a k_split_cluster launch.
 template <typename T, int E>
-size_t cluster_smem(int kw, int l) {
+size_t cluster_smem(int kw, int l, int qb) {
   using F = typename F32<T>::type;
-  const size_t ncs = (size_t)(l + kCW - 1) / kCW;
-  const size_t qr = sizeof(F) * (ncs * (size_t)kw + 2 * (size_t)kw);
+  const size_t qr = qr_bytes<F>(qr_slots(l, qb), kw, qb);
   const size_t rmax = (size_t)(std::min(std::min(kw, l), kMaxRows) + 2 * kCW - 1) / (2 * kCW);
   const size_t jb = sizeof(F) * 6 * rmax * 32 * E;  // 2 blocks + 2 x 2 mailboxes
   return ((std::max(qr, jb) + 15) / 16) * 16 + sizeof(CtrlS);
@@ -152,22 +218,26 @@ __global__ void __launch_bounds__(kCNT, 1)
     k_split_cluster(const T* __restrict__ A, int n_a, int trans, int kw, int l, double thr_rel,
                     double thr_abs, float tol2, int max_sweeps, T* __restrict__ out_rows,
                     double* __restrict__ out_nrm, int kcap, JacobiCtl* ctl_out,
-                    double* __restrict__ info, int qr_cap) {
+                    double* __restrict__ info, int qr_cap, int qb, float* __restrict__ vbuf) {
   using F = typename F32<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gw = rank * kCNW + warp;
-  const int ncs = (l + kCW - 1) / kCW;  // column slots per CTA
+  // column c: block c / qb, held by CTA (c / qb) % 16 in slot
+  // ((c / qb) / 16) qb + c % qb
+  const int ncs = qr_slots(l, qb);  // column slots per CTA
   const int kmax = min(kw, l);
   // a learned rank caps the QR steps (0: the trailing weight alone decides)
   const int qsteps = qr_cap > 0 ? min(kmax, qr_cap) : kmax;
   constexpr int LP = 32 * E;
 
   F* cols = reinterpret_cast<F*>(smem_raw);        // [ncs][kw], phase 1
-  F* refl = cols + (size_t)ncs * kw;               // [2][kw]
-  const size_t qr = sizeof(F) * ((size_t)ncs * kw + 2 * (size_t)kw);
+  F* refl = cols + qr_cols_elems<F>(ncs, kw);      // reflector blocks, see phase 1
+  const int ks = kw | 1;                           // column stride
+  const size_t qr = qr_bytes<F>(ncs, kw, qb);
+  auto col_of = [&](int s) { return ((s / qb) * kCW + rank) * qb + s % qb; };
   const size_t rmax = (size_t)(min(kmax, kMaxRows) + 2 * kCW - 1) / (2 * kCW);
   const size_t jb = sizeof(F) * 6 * rmax * LP;
   CtrlS* ctrl = reinterpret_cast<CtrlS*>(smem_raw + ((max(qr, jb) + 15) / 16) * 16);
@@ -183,7 +253,7 @@ __global__ void __launch_bounds__(kCNT, 1)
   {
     double acc = 0.0;
     for (int s = warp; s < ncs; s += kCNW) {
-      const int c = rank + s * kCW;
+      const int c = col_of(s);
       if (c >= l) break;
       for (int i = lane; i < kw; i += 32) acc += S<T>::abs2(Wat(i, c));
     }
@@ -204,105 +274,378 @@ __global__ void __launch_bounds__(kCNT, 1)
   // stop once the trailing block holds at most max(thr_rel |W|^2, thr_abs)
   const float thr = (float)fmax(thr_rel, norm2 > 0.0 ? thr_abs / norm2 : 0.0);
   for (int s = warp; s < ncs; s += kCNW) {
-    const int c = rank + s * kCW;
+    const int c = col_of(s);
     if (c >= l) break;
-    for (int i = lane; i < kw; i += 32) cols[(size_t)s * kw + i] = F32<T>::from(Wat(i, c), scale);
+    for (int i = lane; i < kw; i += 32) cols[(size_t)s * ks + i] = F32<T>::from(Wat(i, c), scale);
   }
   __syncthreads();
 
-  // ---- phase 1: rank-revealing Householder QR --------------------------------
-  // Reflector from x = col[j:kw): v = x + nu e1, nu = (x0/|x0|)|x|,
-  // tau = 1/(|x|(|x|+|x0|)); col[j] <- -nu.  `xn2` = |x|^2.  One warp.
-  auto make_reflector = [&](F* col, int j, float xn2, F* vdst, float* tau_dst) {
-    const float xn = sqrtf(xn2);
-    const F x0 = col[j];
-    const float a0 = sqrtf(f_abs2(x0));
-    float pr = 1.f, pi = 0.f;  // phase of x0
-    if (a0 > 0.f) {
-      pr = f_re(x0) / a0;
-      pi = f_im(x0) / a0;
-    }
-    for (int i = j + 1 + lane; i < kw; i += 32) vdst[i] = col[i];
-    __syncwarp();  // every lane has read x0 before lane 0 overwrites it
-    if (lane == 0) {
-      F v0;
-      f_set(v0, f_re(x0) + pr * xn, f_im(x0) + pi * xn);
-      vdst[j] = v0;
-      *tau_dst = xn > 0.f ? 1.0f / (xn * (xn + a0)) : 0.f;
-      F d;
-      f_set(d, -pr * xn, -pi * xn);
-      col[j] = d;
+  // ---- phase 1: rank-revealing blocked Householder QR -------------------------
+  // Row `row` of a block of reflectors (qb entries, 128-bit loads when qb = 8).
+  constexpr int NV4 = kQB * (int)sizeof(F) / 16;
+  auto load_vrow = [&](const F* Vp, int row, F* v) {
+    if (qb == kQB) {
+      const float4* s4 = reinterpret_cast<const float4*>(Vp + (size_t)row * kQB);
+#pragma unroll
+      for (int u = 0; u < NV4; ++u) unpack4(s4[u], v + u * (4 / (int)(sizeof(F) / 4)));
+    } else {
+#pragma unroll
+      for (int i = 0; i < kQB; ++i) v[i] = i < qb ? Vp[(size_t)row * qb + i] : F32<T>::zero();
     }
   };
-  // The owner CTA of the next reflector pushes it (and tau) into every other
-  // CTA's buffer of that parity before the barrier; the trailing-weight
-  // partials are pushed to every CTA the same way, so after the barrier all
-  // reads are local.
-  auto push_reflector = [&](int j, int par) {  // all threads of the owner CTA
-    F* v = refl + (size_t)par * kw;
-    for (int r = 0; r < kCW; ++r) {
-      if (r == rank) continue;
-      F* d = cluster.map_shared_rank(v, r);
-      for (int i = j + tid; i < kw; i += kCNT) d[i] = v[i];
+  const int kwp = (kw + 3) & ~3;  // rows of a reflector block buffer (16-byte multiple)
+  F* Vb = refl;                              // [2][kwp][qb]
+  F* Tm = Vb + (size_t)2 * kwp * qb;         // [2][kQB][kQB]
+  F* ys = Tm + (size_t)2 * kQB * kQB;        // [16][qb][32]: y partials of the block update
+  F* ysum = ys + (size_t)kCNW * qb * 32;     // [qb][32]
+  float* ebin = reinterpret_cast<float*>(ysum + (size_t)qb * 32);  // [qb][32]
+  float* tl = ebin + (size_t)qb * 32;                                // [16][32]
+  // Every live column of this CTA (col >= c0 + nb) through the block of nb
+  // reflectors in compact WY form (H_{nb-1} .. H_0 = I - V T^H V^H, Vp
+  // row-major [row][qb], Tp = T [8][8] upper triangular): y = V^H col,
+  // z = T^H y, col -= V z on rows c0..kw-1.  Lane j owns column slot 32 g + j,
+  // warp w the rows c0 + w + 16 t.  acc[i] (all lanes of warp 0) gains the
+  // weights below the block's steps, the sum over the live columns of
+  // |col[c0+i+1:kw)|^2.  All threads; ends with a CTA barrier.
+  auto update_block = [&](const F* Vp, const F* Tp, int c0, int nb, float* acc) {
+    for (int g = 0; g * 32 < ncs; ++g) {
+      const int sl = g * 32 + lane;
+      const int c = sl < ncs ? col_of(sl) : l;
+      const bool live = c < l && c >= c0 + nb;
+      F* col = cols + (size_t)(live ? sl : 0) * ks;
+      float yr[kQB], yi[kQB];
+#pragma unroll
+      for (int i = 0; i < kQB; ++i) yr[i] = yi[i] = 0.f;
+      for (int row = c0 + warp; row < kw; row += kCNW) {
+        F v[kQB];
+        load_vrow(Vp, row, v);
+        const F x = live ? col[row] : F32<T>::zero();
+#pragma unroll
+        for (int i = 0; i < kQB; ++i)
+          if (i < nb) f_dotc(v[i], x, yr[i], yi[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < kQB; ++i)
+        if (i < nb) f_set(ys[((size_t)warp * qb + i) * 32 + lane], yr[i], yi[i]);
+      __syncthreads();
+      if (tid < nb * 32) {  // fixed-order sum over the warps
+        float sr = 0.f, si = 0.f;
+        for (int w = 0; w < kCNW; ++w) {
+          const F t = ys[(size_t)w * qb * 32 + tid];
+          sr += f_re(t);
+          si += f_im(t);
+        }
+        f_set(ysum[tid], sr, si);
+      }
+      __syncthreads();
+      float zr[kQB], zi[kQB];  // z_k = sum_{i <= k} conj(T_ik) y_i
+#pragma unroll
+      for (int k = 0; k < kQB; ++k) {
+        zr[k] = zi[k] = 0.f;
+#pragma unroll
+        for (int i = 0; i <= k; ++i) {
+          if (i < nb && k < nb) {
+            const F t = Tp[i * kQB + k];
+            const F y = ysum[i * 32 + lane];
+            zr[k] = fmaf(f_re(t), f_re(y), fmaf(f_im(t), f_im(y), zr[k]));
+            zi[k] = fmaf(f_re(t), f_im(y), fmaf(-f_im(t), f_re(y), zi[k]));
+          }
+        }
+      }
+      float tail = 0.f;
+      for (int row = c0 + warp; row < kw; row += kCNW) {
+        F v[kQB];
+        load_vrow(Vp, row, v);
+        F x = live ? col[row] : F32<T>::zero();
+#pragma unroll
+        for (int i = 0; i < kQB; ++i)
+          if (i < nb) f_axpy(zr[i], zi[i], v[i], x);
+        if (live) col[row] = x;
+        const float x2 = f_abs2(x);
+        if (row >= c0 + nb) tail += x2;
+        else if (row > c0) ebin[(row - c0) * 32 + lane] = x2;  // rows c0+1 .. c0+nb-1
+      }
+      tl[warp * 32 + lane] = tail;
+      __syncthreads();
+      if (warp == 0) {
+        float run = 0.f;  // S(nb-1) = the tail, S(i) = S(i+1) + |col[c0+i+1]|^2
+        for (int w = 0; w < kCNW; ++w) run += tl[w * 32 + lane];
+#pragma unroll
+        for (int i = kQB - 1; i >= 0; --i) {
+          if (i < nb) {
+            acc[i] += warp_sum(run);
+            if (i >= 1) run += ebin[i * 32 + lane];
+          }
+        }
+      }
+      __syncthreads();
     }
-    if (tid < kCW && tid != rank) cluster.map_shared_rank(ctrl, tid)->tau[par] = ctrl->tau[par];
   };
-  if (rank == 0 && warp == 0 && l > 0) {
-    float xn2 = 0.f;
-    for (int i = lane; i < kw; i += 32) xn2 += f_abs2(cols[i]);
-    xn2 = warp_sum(xn2);
-    make_reflector(cols, 0, xn2, refl, &ctrl->tau[0]);
+  auto Vpar = [&](int p) { return Vb + (size_t)p * kwp * qb; };
+  auto Tpar = [&](int p) { return Tm + (size_t)p * kQB * kQB; };
+  // Panel of the owner CTA: columns cp .. cp+nbp-1 (slots sp ..), warp k owns
+  // column cp + k.  Writes the block of reflectors (rows cp.., zero above each
+  // reflector's first row) into Vpar(p), its T factor into Tpar(p), and the
+  // in-panel weights inpanel[k][i] = |R[cp+i+1 .. cp+k, cp+k]|^2 (i < k).
+  // Panel of the owner CTA: columns cp .. cp+nbp-1 (slots sp ..), factored by
+  // the whole CTA.  Thread t holds rows t and t + 512 of the panel's columns
+  // in registers; each reflector is two CTA-wide sums (the column norm with
+  // the reflector Gram entries it completes, then v^H of the later columns).
+  // Reflector i (pivot row j = cp + i): v = x + nu e_j, nu = (x_j/|x_j|)|x|,
+  // tau = 1/(|x|(|x|+|x_j|)), x_j <- -nu, x = rows j..kw-1 of column i; v is
+  // zero above row j.  Writes the block of reflectors into Vpar(p), its T
+  // factor into Tpar(p), the R entries back into the columns, and the
+  // in-panel weights inpanel[k][i] = |R[cp+i+1 .. cp+k, cp+k]|^2 (i < k).
+  auto factor_panel = [&](int cp, int nbp, int sp, int p) {
+    F x[kPanelRP][kQB];
+    F v0s[kQB];
+    float taus[kQB];
+#pragma unroll
+    for (int pr = 0; pr < kPanelRP; ++pr) {
+      const int row = tid + kCNT * pr;
+#pragma unroll
+      for (int k = 0; k < kQB; ++k)
+        x[pr][k] = (k < nbp && row >= cp && row < kw) ? cols[(size_t)(sp + k) * ks + row]
+                                                      : F32<T>::zero();
+    }
+#pragma unroll
+    for (int i = 0; i < kQB; ++i) {
+      v0s[i] = F32<T>::zero();
+      taus[i] = 0.f;
+    }
+    // v_m on a row below its pivot is the column's stored value
+#pragma unroll
+    for (int i = 0; i < kQB; ++i) {
+      if (i < nbp) {
+      const int j = cp + i;
+      // the pivot row's values: x_i[j] and v_m[j] = x_m[j] (m < i)
+#pragma unroll
+      for (int pr = 0; pr < kPanelRP; ++pr)
+        if (tid + kCNT * pr == j) {
+#pragma unroll
+          for (int m = 0; m <= i; ++m) ctrl->prow[m] = make_float2(f_re(x[pr][m]), f_im(x[pr][m]));
+        }
+      // |x_i|^2 over rows >= j; sum over rows > j of conj(v_m) x_i (m < i)
+      float red[16];
+#pragma unroll
+      for (int a = 0; a < 16; ++a) red[a] = 0.f;
+#pragma unroll
+      for (int pr = 0; pr < kPanelRP; ++pr) {
+        const int row = tid + kCNT * pr;
+        if (row >= j && row < kw) red[0] += f_abs2(x[pr][i]);
+        if (row > j && row < kw) {
+#pragma unroll
+          for (int m = 0; m < i; ++m) {
+            float gr = 0.f, gi = 0.f;
+            f_dotc(x[pr][m], x[pr][i], gr, gi);
+            red[1 + 2 * m] += gr;
+            red[2 + 2 * m] += gi;
+          }
+        }
+      }
+      cta_sum(ctrl, red, 1 + 2 * i);
+      const float2 xp = ctrl->prow[i];
+      F x0;
+      f_set(x0, xp.x, xp.y);
+      const float xn = sqrtf(red[0]);
+      const float a0 = sqrtf(f_abs2(x0));
+      float pr_ = 1.f, pi_ = 0.f;  // phase of x_j
+      if (a0 > 0.f) {
+        pr_ = f_re(x0) / a0;
+        pi_ = f_im(x0) / a0;
+      }
+      f_set(v0s[i], f_re(x0) + pr_ * xn, f_im(x0) + pi_ * xn);
+      taus[i] = xn > 0.f ? 1.0f / (xn * (xn + a0)) : 0.f;
+      // Gram entries v_m^H v_i = (rows > j) + conj(v_m[j]) v0_i
+      if (tid == 0) {
+#pragma unroll
+        for (int m = 0; m < i; ++m) {
+          const float2 vm = ctrl->prow[m];
+          const float gr = red[1 + 2 * m] + vm.x * f_re(v0s[i]) + vm.y * f_im(v0s[i]);
+          const float gi = red[2 + 2 * m] + vm.x * f_im(v0s[i]) - vm.y * f_re(v0s[i]);
+          ctrl->gram[m][i] = make_float2(gr, gi);
+        }
+      }
+      // v_i on this thread's rows; the pivot row of column i becomes -nu
+      F vi[kPanelRP];
+#pragma unroll
+      for (int pr = 0; pr < kPanelRP; ++pr) {
+        const int row = tid + kCNT * pr;
+        vi[pr] = (row > j && row < kw) ? x[pr][i] : (row == j ? v0s[i] : F32<T>::zero());
+        if (row == j) f_set(x[pr][i], -pr_ * xn, -pi_ * xn);
+      }
+      // d_k = v_i^H x_k (k > i), then x_k -= tau d_k v_i
+      float dd[16];
+#pragma unroll
+      for (int a = 0; a < 16; ++a) dd[a] = 0.f;
+#pragma unroll
+      for (int pr = 0; pr < kPanelRP; ++pr) {
+#pragma unroll
+        for (int k = i + 1; k < kQB; ++k) {
+          float gr = 0.f, gi = 0.f;
+          f_dotc(vi[pr], x[pr][k], gr, gi);
+          dd[2 * k] += gr;
+          dd[2 * k + 1] += gi;
+        }
+      }
+      cta_sum(ctrl, dd, 2 * nbp);
+#pragma unroll
+      for (int k = i + 1; k < kQB; ++k) {
+        const float wr = taus[i] * dd[2 * k], wi = taus[i] * dd[2 * k + 1];
+#pragma unroll
+        for (int pr = 0; pr < kPanelRP; ++pr) f_axpy(wr, wi, vi[pr], x[pr][k]);
+      }
+    }
+    }
+    // R entries and reflectors back to shared memory
+    F* Vp = Vpar(p);
+#pragma unroll
+    for (int pr = 0; pr < kPanelRP; ++pr) {
+      const int row = tid + kCNT * pr;
+      if (row >= cp && row < kw) {
+#pragma unroll
+        for (int k = 0; k < kQB; ++k) {
+          if (k < nbp) cols[(size_t)(sp + k) * ks + row] = x[pr][k];
+          if (k < qb) {
+            const int jk = cp + k;
+            const F v = k >= nbp ? F32<T>::zero()
+                                 : (row > jk ? x[pr][k] : (row == jk ? v0s[k] : F32<T>::zero()));
+            Vp[(size_t)row * qb + k] = v;
+          }
+        }
+        // |R[row][cp+k]|^2 for the rows just below the block's first row
+        const int rr = row - cp;
+        if (rr >= 1 && rr < kQB) {
+#pragma unroll
+          for (int k = 0; k < kQB; ++k) ctrl->rsq[rr][k] = (k < nbp && k >= rr) ? f_abs2(x[pr][k]) : 0.f;
+        }
+      }
+    }
+    __syncthreads();
+    // inpanel[k][i] = sum_{r=i+1}^{k} |R[cp+r][cp+k]|^2 ; T row i (lane i of warp 0):
+    // T_kk = tau_k, T[0:k, k] = -tau_k T[0:k, 0:k] gram[0:k, k]
+    if (warp == 0 && lane < kQB) {
+      const int i = lane;
+#pragma unroll
+      for (int k = 0; k < kQB; ++k) {
+        float t = 0.f;
+        for (int r = i + 1; r <= k && r < kQB; ++r) t += ctrl->rsq[r][k];
+        ctrl->inpanel[k][i] = (k < nbp && i < k) ? t : 0.f;
+      }
+      F* Tp = Tpar(p);
+      float tre[kQB], tim[kQB];
+#pragma unroll
+      for (int k = 0; k < kQB; ++k) {
+        float tr = 0.f, ti = 0.f;
+        if (k < nbp) {
+          if (i == k) {
+            tr = taus[k];
+          } else if (i < k) {
+            float sr = 0.f, si = 0.f;  // sum_{m=i}^{k-1} T_im gram_mk
+#pragma unroll
+            for (int m = 0; m < k; ++m) {
+              if (m >= i) {
+                const float2 g = ctrl->gram[m][k];
+                sr += tre[m] * g.x - tim[m] * g.y;
+                si += tre[m] * g.y + tim[m] * g.x;
+              }
+            }
+            tr = -taus[k] * sr;
+            ti = -taus[k] * si;
+          }
+        }
+        tre[k] = tr;
+        tim[k] = ti;
+        f_set(Tp[i * kQB + k], tr, ti);
+      }
+    }
+  };
+  // The owner of a block writes its reflector block (rows from the block's
+  // first row) and T to the global buffer of that parity; every other CTA
+  // copies them into its own shared memory after the barrier (L2 loads: the
+  // buffer is rewritten every other block).
+  F* vg = reinterpret_cast<F*>(vbuf);
+  auto Gpar = [&](int p) { return vg + (size_t)p * ((size_t)kwp * qb + kQB * kQB); };
+  const int nt4 = kQB * kQB * (int)sizeof(F) / 16;
+  auto publish = [&](int cp, int p) {  // all threads of the owner CTA
+    const int b0 = (int)((size_t)cp * qb * sizeof(F) / 16);
+    const int b1 = (int)((size_t)kwp * qb * sizeof(F) / 16);
+    float4* g = reinterpret_cast<float4*>(Gpar(p));
+    const float4* src = reinterpret_cast<const float4*>(Vpar(p));
+    for (int f = b0 + tid; f < b1; f += kCNT) g[f] = src[f];
+    float4* gt = reinterpret_cast<float4*>(Gpar(p) + (size_t)kwp * qb);
+    if (tid < nt4) gt[tid] = reinterpret_cast<const float4*>(Tpar(p))[tid];
+  };
+  auto fetch = [&](int cp, int p) {  // all threads of every other CTA
+    const int b0 = (int)((size_t)cp * qb * sizeof(F) / 16);
+    const int b1 = (int)((size_t)kwp * qb * sizeof(F) / 16);
+    const float4* g = reinterpret_cast<const float4*>(Gpar(p));
+    float4* dst = reinterpret_cast<float4*>(Vpar(p));
+    for (int f = b0 + tid; f < b1; f += kCNT) dst[f] = __ldcg(g + f);
+    const float4* gt = reinterpret_cast<const float4*>(Gpar(p) + (size_t)kwp * qb);
+    if (tid < nt4) reinterpret_cast<float4*>(Tpar(p))[tid] = __ldcg(gt + tid);
+    __syncthreads();
+  };
+  auto slot_of = [&](int c) { return ((c / qb) / kCW) * qb + c % qb; };
+  // block 0: factored by CTA 0 before the first barrier
+  const int nb0 = min(qb, qsteps);
+  if (rank == 0 && nb0 > 0) {
+    factor_panel(0, nb0, 0, 0);
+    __syncthreads();
+    publish(0, 0);
   }
-  __syncthreads();
-  if (rank == 0 && l > 0) push_reflector(0, 0);
   cluster.sync();
   int keff = qsteps;
   float trail = 0.f;
-  for (int j = 0; j < qsteps; ++j) {
-    const int par = j & 1;
-    const F* v = refl + (size_t)par * kw;
-    const float tau = ctrl->tau[par];
-    float tw = 0.f;  // this warp's trailing weight
-    for (int s = warp; s < ncs; s += kCNW) {
-      const int c = rank + s * kCW;
-      if (c >= l) break;
-      if (c <= j) continue;
-      F* col = cols + (size_t)s * kw;
-      float dr = 0.f, di = 0.f;
-      for (int i = j + lane; i < kw; i += 32) f_dotc(v[i], col[i], dr, di);
-      dr = warp_sum(dr);
-      di = warp_sum(di);
-      const float wr = tau * dr, wi = tau * di;
-      float cn = 0.f;
-      for (int i = j + lane; i < kw; i += 32) {
-        F x = col[i];
-        f_axpy(wr, wi, v[i], x);
-        col[i] = x;
-        if (i > j) cn += f_abs2(x);
-      }
-      cn = warp_sum(cn);
-      tw += cn;
-      if (c == j + 1 && j + 1 < kmax) {
-        __syncwarp();
-        make_reflector(col, j + 1, cn, refl + (size_t)(par ^ 1) * kw, &ctrl->tau[par ^ 1]);
-      }
+  for (int q = 0; q * qb < qsteps; ++q) {
+    const int par = q & 1;
+    const int c0 = q * qb, nb = min(qb, qsteps - c0);
+    const int c1 = c0 + qb, nb1 = min(qb, qsteps - c1);  // next block (nb1 <= 0: none)
+    const bool owner1 = nb1 > 0 && rank == (q + 1) % kCW;
+    const int sp1 = owner1 ? slot_of(c1) : -1;
+    if (rank != q % kCW) fetch(c0, par);
+    const F* Vq = Vpar(par);
+    const F* Tq = Tpar(par);
+    float acc[kQB];
+#pragma unroll
+    for (int i = 0; i < kQB; ++i) acc[i] = 0.f;
+    update_block(Vq, Tq, c0, nb, acc);
+    if (tid == 0) {
+#pragma unroll
+      for (int i = 0; i < kQB; ++i) ctrl->red[0][i] = acc[i];
     }
-    if (lane == 0) ctrl->red[warp] = tw;
-    __syncthreads();
-    if (j + 1 < kmax && rank == (j + 1) % kCW) push_reflector(j + 1, par ^ 1);
-    if (tid < kCW) {
+    // the next panel, now up to date
+    if (owner1) {
+      factor_panel(c1, nb1, sp1, par ^ 1);
+      __syncthreads();
+      publish(c1, par ^ 1);
+    } else {
+      __syncthreads();
+    }
+    if (tid < kCW * kQB) {  // every CTA receives every partial
+      const int dst = tid / kQB, i = tid % kQB;
       float t = 0.f;
-      for (int w = 0; w < kCNW; ++w) t += ctrl->red[w];
-      cluster.map_shared_rank(ctrl, tid)->part[par][rank] = t;
+      if (i < nb) {
+        t = ctrl->red[0][i];
+        // the block's own panel (factored by this CTA in the previous step)
+        if (rank == q % kCW)
+          for (int k = 0; k < nb; ++k) t += ctrl->inpanel[k][i];
+      }
+      cluster.map_shared_rank(ctrl, dst)->part[par][rank][i] = t;
     }
     cluster.sync();
-    float t = 0.f;
-    for (int r = 0; r < kCW; ++r) t += ctrl->part[par][r];
-    trail = t;
-    if (t <= thr) {
-      keff = j + 1;
-      break;
+    bool stop = false;
+    for (int i = 0; i < nb; ++i) {
+      float t = 0.f;
+      for (int r = 0; r < kCW; ++r) t += ctrl->part[par][r][i];
+      trail = t;
+      if (t <= thr) {
+        keff = c0 + i + 1;
+        stop = true;
+        break;
+      }
     }
+    if (stop) break;
   }
   const unsigned long long t_qr = global_ns();
 
@@ -327,7 +670,7 @@ __global__ void __launch_bounds__(kCNT, 1)
         const int half = f / blk, ri = (f % blk) / LP, x = f % LP;
         const int i = (half ? 2 * kCW - 1 - rank : rank) * r + ri;
         if (i < keff && x < l && x >= i)
-          tmp[u] = cluster.map_shared_rank(cols + (size_t)(x / kCW) * kw, x % kCW)[i];
+          tmp[u] = cluster.map_shared_rank(cols + (size_t)slot_of(x) * ks, (x / qb) % kCW)[i];
       }
     }
     cluster.sync();  // column storage is dead from here on
@@ -536,10 +879,20 @@ __global__ void __launch_bounds__(kCNT, 1)
   cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
+// The widest QR column block (8, 4, 2 or 1) whose shared memory fits.
 template <typename T, int E>
-bool cluster_config(int kw, int l, size_t* smem_out) {
-  const size_t smem = cluster_smem<T, E>(kw, l);
-  if (smem > 227 * 1024) return false;
+int pick_qb(int kw, int l) {
+  for (int qb = kQB; qb >= 1; qb /= 2)
+    if (cluster_smem<T, E>(kw, l, qb) <= 227 * 1024) return qb;
+  return 0;
+}
+
+template <typename T, int E>
+bool cluster_config(int kw, int l, size_t* smem_out, int* qb_out) {
+  const int qb = pick_qb<T, E>(kw, l);
+  if (qb == 0) return false;
+  const size_t smem = cluster_smem<T, E>(kw, l, qb);
+  *qb_out = qb;
   auto fn = k_split_cluster<T, E>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
       raise_smem_limit(fn, smem) != SM_OK) {
@@ -569,9 +922,11 @@ bool cluster_config(int kw, int l, size_t* smem_out) {
 template <typename T, int E>
 int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw, int l,
                          double thr_rel, double thr_abs, int max_sweeps, T* out_rows,
-                         double* out_nrm, int kcap, JacobiCtl* ctl, double* info, int qr_cap) {
+                         double* out_nrm, int kcap, JacobiCtl* ctl, double* info, int qr_cap,
+                         float* vbuf) {
   size_t smem = 0;
-  if (!cluster_config<T, E>(kw, l, &smem)) {
+  int qb = 0;
+  if (!cluster_config<T, E>(kw, l, &smem, &qb)) {
     set_error("mixed split: cluster configuration not available");
     return SM_ERR_VALUE;
   }
@@ -591,7 +946,7 @@ int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw
   const float tol2 = (float)l * eps * eps;
   SM_CUDA_CHECK(cudaLaunchKernelEx(&cfg, k_split_cluster<T, E>, A, n_a, trans, kw, l, thr_rel,
                                    thr_abs, tol2, max_sweeps, out_rows, out_nrm, kcap, ctl,
-                                   info, qr_cap));
+                                   info, qr_cap, qb, vbuf));
   note_launch();
   return SM_OK;
 }
@@ -611,26 +966,28 @@ inline int e_bucket(int l) {
 
 template <typename T>
 bool split_cluster_fits(int kw, int l) {
-  if (std::min(kw, l) > kMaxRows || kw > 1024) return false;
+  // the QR panel holds kPanelRP rows per thread in registers
+  if (std::min(kw, l) > kMaxRows || kw > kCNT * kPanelRP) return false;
   const int e = e_bucket(l);
   if (e == 0) return false;
   if (sizeof(T) != sizeof(double) && e > 16) return false;  // complex rows beyond 512 spill
   // Residency is checked once per (dtype, E): the answer does not depend on
   // the sizes beyond the shared-memory amount, which is re-checked below.
   size_t smem = 0;
+  int qb = 0;
   switch (e) {
-    case 4: return cluster_config<T, 4>(kw, l, &smem);
-    case 8: return cluster_config<T, 8>(kw, l, &smem);
-    case 12: return cluster_config<T, 12>(kw, l, &smem);
-    case 16: return cluster_config<T, 16>(kw, l, &smem);
-    default: return cluster_config<T, 24>(kw, l, &smem);
+    case 4: return cluster_config<T, 4>(kw, l, &smem, &qb);
+    case 8: return cluster_config<T, 8>(kw, l, &smem, &qb);
+    case 12: return cluster_config<T, 12>(kw, l, &smem, &qb);
+    case 16: return cluster_config<T, 16>(kw, l, &smem, &qb);
+    default: return cluster_config<T, 24>(kw, l, &smem, &qb);
   }
 }
 
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, int qr_cap) {
+                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf) {
   // W = A^T (kw = n, l = m) when U is wanted, else W = A (kw = m, l = n)
   const int kw = want_u ? n : m;
   const int l = want_u ? m : n;
@@ -639,7 +996,7 @@ int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, do
 #define SM_C(EV)                                                                              \
   case EV:                                                                                    \
     return launch_split_cluster<T, EV>(st, A, n, trans, kw, l, thr_rel, thr_abs, max_sweeps, \
-                                       out_rows, out_nrm, kcap, ctl, info, qr_cap)
+                                       out_rows, out_nrm, kcap, ctl, info, qr_cap, vbuf)
     SM_C(4);
     SM_C(8);
     SM_C(12);
@@ -657,8 +1014,13 @@ template bool split_cluster_fits<double>(int, int);
 template bool split_cluster_fits<cplx>(int, int);
 template int split_cluster_f32<double>(cudaStream_t, const double*, int, int, bool, double,
                                        double, int, double*, double*, int, JacobiCtl*, double*,
-                                       int);
+                                       int, float*);
 template int split_cluster_f32<cplx>(cudaStream_t, const cplx*, int, int, bool, double, double,
-                                     int, cplx*, double*, int, JacobiCtl*, double*, int);
+                                     int, cplx*, double*, int, JacobiCtl*, double*, int, float*);
+
+size_t split_cluster_vbuf_floats(int kw) {
+  // two parities of a reflector block [kwp][8] and its T [8][8], complex
+  return (size_t)2 * (((size_t)(kw + 3) & ~(size_t)3) * kQB + kQB * kQB) * 2;
+}
 
 }  // namespace sm

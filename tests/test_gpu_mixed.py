@@ -137,7 +137,7 @@ def test_mixed_split_against_oracle(mixed, cplx, case, side):
 
 @pytest.mark.parametrize("cplx", [False, True])
 @pytest.mark.parametrize("want_u", [0, 1])
-@pytest.mark.parametrize("shape", [(96, 64), (64, 200), (320, 320)])
+@pytest.mark.parametrize("shape", [(96, 64), (64, 200), (320, 320), (512, 256)])
 def test_cluster_rows_span_and_orthogonality(cplx, want_u, shape):
     """FP32 stage alone: rows mutually orthogonal to FP32 accuracy, Y^H Y = W^H W
     (same row space and singular values) to FP32 accuracy."""
