@@ -172,17 +172,26 @@ struct CtrlS {
   double red64[kCNW];
 };
 
-// CTA-wide sum of n <= 16 floats (every thread gets the sums; fixed order).
+// CTA-wide sum of 16 floats (entries n.. must be zero; every thread gets the
+// sums; fixed order).  Within a warp a butterfly that halves the values it
+// carries at each level (16 shuffles for the 16 sums): lanes 2a and 2a+1 end
+// with the warp's sum of value a.
 __device__ __forceinline__ void cta_sum(CtrlS* ctrl, float (&v)[16], int n) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
-  for (int a = 0; a < 16; ++a)
-    if (a < n) v[a] = warp_sum(v[a]);
-  if (lane == 0) {
+  for (int h = 8, o = 16; h >= 1; h >>= 1, o >>= 1) {
+    const bool up = (lane & o) != 0;
 #pragma unroll
-    for (int a = 0; a < 16; ++a)
-      if (a < n) ctrl->pred[warp][a] = v[a];
+    for (int a = 0; a < 8; ++a) {
+      if (a < h) {
+        const float keep = up ? v[a + h] : v[a];
+        const float send = up ? v[a] : v[a + h];
+        v[a] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+    }
   }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+  if ((lane & 1) == 0 && (lane >> 1) < n) ctrl->pred[warp][lane >> 1] = v[0];
   __syncthreads();
   if (tid < n) {
     float t = 0.f;
