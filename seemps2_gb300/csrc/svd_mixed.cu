@@ -146,6 +146,14 @@ __device__ __forceinline__ void unpack4(float4 t, float2* v) {
   v[1] = make_float2(t.z, t.w);
 }
 
+// tan of the Jacobi angle, 1 / (|zeta| + sqrt(1 + zeta^2)), with the SFU's
+// approximate reciprocal square root and reciprocal (a few ulp; the rotation
+// built from it is orthogonal to FP32 rounding whatever the angle's error)
+__device__ __forceinline__ float rot_tan(float az) {
+  const float q = fmaf(az, az, 1.0f);
+  return __fdividef(1.0f, fmaf(q, rsqrtf(q), az));
+}
+
 __device__ __forceinline__ float warp_sum(float x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -325,6 +333,7 @@ __global__ void __launch_bounds__(kCNT, 1)
       float yr[kQB], yi[kQB];
 #pragma unroll
       for (int i = 0; i < kQB; ++i) yr[i] = yi[i] = 0.f;
+#pragma unroll 2
       for (int row = c0 + warp; row < kw; row += kCNW) {
         F v[kQB];
         load_vrow(Vp, row, v);
@@ -362,6 +371,7 @@ __global__ void __launch_bounds__(kCNT, 1)
         }
       }
       float tail = 0.f;
+#pragma unroll 2
       for (int row = c0 + warp; row < kw; row += kCNW) {
         F v[kQB];
         load_vrow(Vp, row, v);
@@ -734,7 +744,7 @@ __global__ void __launch_bounds__(kCNT, 1)
     const float zeta = 0.5f * (b - a) * rg;
     const float az = fabsf(zeta);
     const float tt =
-        copysignf(az < 1e18f ? __frcp_rn(az + sqrtf(fmaf(az, az, 1.0f))) : 0.5f / az, zeta);
+        copysignf(az < 1e18f ? rot_tan(az) : 0.5f / az, zeta);
     const float c = rsqrtf(fmaf(tt, tt, 1.0f));
     const float sn = c * tt;
     const float ar = sn * gr * rg, ai = sn * gi * rg;  // s e
