@@ -345,6 +345,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 
 // One operand of the preparation kernels: op(X) is rows x K with element
 // (r, k) = X[r * ldx + k] (trans = 0) or X[k * ldx + r] (trans = 1).
+constexpr int kOzNoExp = (int)0x80808080;  // exponent of an all-zero row
+
 struct OzOperand {
   const double* X;
   int ldx, rows, trans;
@@ -353,17 +355,16 @@ struct OzOperand {
 };
 
 // Exponent e (x = f 2^e, f in [0.5, 1)) of the largest |element| of each row
-// of op(X), by atomicMax over 256-wide K ranges (blockIdx.y) into ex, which
-// starts at the bytes 0x80 (no element seen: an all-zero row).  32 x 32
-// threads per 32 rows and K range; lanes run along the contiguous index;
-// blockIdx.z picks the operand.
+// of op(X) into ex; the bytes 0x80 (kOzNoExp) for an all-zero (or non-finite)
+// row.  32 x 32 threads per 32 rows over the whole of K; lanes run along the
+// contiguous index; blockIdx.z picks the operand.
 __global__ void __launch_bounds__(1024) k_oz_exp(OzOperand A, OzOperand B, int K) {
   const OzOperand& o = blockIdx.z ? B : A;
   __shared__ double red[32][33];
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 32
   const int r0 = blockIdx.x * 32;
   if (r0 >= o.rows) return;  // uniform over the block
-  const int k0 = blockIdx.y * 256, k1 = min(K, k0 + 256);
+  const int k0 = 0, k1 = K;
   double m = 0.0;
   if (o.trans) {  // tx = row, ty strides over k
     const int r = r0 + tx;
@@ -381,10 +382,10 @@ __global__ void __launch_bounds__(1024) k_oz_exp(OzOperand A, OzOperand B, int K
     double v = 0.0;
     for (int j = 0; j < 32; ++j) v = fmax(v, red[j][tx]);
     const int r = r0 + tx;
-    if (r < o.rows && v > 0.0 && v <= DBL_MAX) {
-      int e = 0;
-      frexp(v, &e);
-      atomicMax(o.ex + r, e);
+    if (r < o.rows) {
+      int e = kOzNoExp;
+      if (v > 0.0 && v <= DBL_MAX) frexp(v, &e);
+      o.ex[r] = e;
     }
   }
 }
@@ -514,10 +515,8 @@ int gemm_oz(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, do
   // (N) or B[n][k] (T, C)
   const int ta = opA == SM_OP_N ? 0 : 1, tb = opB == SM_OP_N ? 1 : 0;
   const OzOperand oa{A, lda, M, ta, ea, sa}, ob{B, ldb, N, tb, eb, sb};
-  SM_CUDA_CHECK(cudaMemsetAsync(ea, 0x80, sizeof(int) * (size_t)M, st));
-  SM_CUDA_CHECK(cudaMemsetAsync(eb, 0x80, sizeof(int) * (size_t)N, st));
   const int rb = (std::max(M, N) + 31) / 32;
-  k_oz_exp<<<dim3(rb, (K + 255) / 256, 2), dim3(32, 32), 0, st>>>(oa, ob, K);
+  k_oz_exp<<<dim3(rb, 1, 2), dim3(32, 32), 0, st>>>(oa, ob, K);
   k_oz_slice<<<dim3(kp / 32, rb, 2), dim3(32, 8), 0, st>>>(oa, ob, K, kp);
   note_launch(2);
   SM_CUDA_CHECK(cudaGetLastError());
@@ -525,10 +524,11 @@ int gemm_oz(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, do
   SM_CHECK(make_slice_map(&mA, sa, M, kp, OM));
   SM_CHECK(make_slice_map(&mB, sb, N, kp, ON));
   const int tiles = ((M + OM - 1) / OM) * ((N + ON - 1) / ON);
-  // split K in whole exact chunks while the output has fewer tiles than SMs
-  const int nch = (nslabs + kChunkSlabs - 1) / kChunkSlabs;
-  int nz = std::max(1, std::min(std::max(1, ctx.num_sms) / tiles, nch));
-  const int slabs_per = ((nch + nz - 1) / nz) * kChunkSlabs;
+  // split K over CTAs while the output has fewer tiles than SMs, in whole
+  // 32-wide slabs, at least two per CTA (each CTA's range is accumulated in
+  // exact chunks of at most 256, so any slab split is exact)
+  int nz = std::max(1, std::min(std::max(1, ctx.num_sms) / tiles, nslabs / 2));
+  const int slabs_per = (nslabs + nz - 1) / nz;
   nz = (nslabs + slabs_per - 1) / slabs_per;
   double* part = nullptr;
   if (nz > 1) SM_CHECK(ctx.scratch("oz.part", (size_t)nz * M * N, &part));
