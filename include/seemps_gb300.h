@@ -327,6 +327,20 @@ enum { SM_MATVEC_FP64 = 0, SM_MATVEC_FP64TC = 1, SM_MATVEC_TF32X3 = 2, SM_MATVEC
 int sm_two_site_matvec(void* ctx, int dtype, const int* dims, const void* L, const void* H,
                        const void* R, const void* v, void* out, int precision, void* stream);
 
+/* Prepared two-site matvec for a Lanczos run (real FP64 operands; precision
+ * SM_MATVEC_TF32X3 or SM_MATVEC_BF16).  sm_two_site_prepare converts L and R
+ * (dims as above) into tensor-core operand planes held by the context; the
+ * caller keeps L and R alive and unchanged until the next prepare.
+ * sm_two_site_matvec_prepared then computes out from H and v with only v
+ * converted per call, X1 kept in FP32 and the MPO step writing the second
+ * product's operand directly (the same operator as sm_two_site_matvec; the
+ * reference applies its matvec to a fixed operator in the same way,
+ * operators/quadratic.py:187-237 inside eigsh, optimization/dmrg.py:15-23). */
+int sm_two_site_prepare(void* ctx, const int* dims, const void* L, const void* R, int precision,
+                        void* stream);
+int sm_two_site_matvec_prepared(void* ctx, const void* H, const void* v, void* out,
+                                void* stream);
+
 /* Upper bound on the bond dimensions a simplify of these kets can produce:
  * min(max_bond_dimension, summed ket bond); fills cap_bonds (L+1). */
 int sm_simplify_bond_caps(int L, const int* phys, int nterms, const int* ket_bonds,

@@ -114,6 +114,8 @@ SIGNATURES = {
     "sm_ctx_set_concurrent": (C.c_int, [vp, C.c_int]),
     "sm_ctx_set_rank_cap": (C.c_int, [vp, C.c_double, C.c_int]),
     "sm_two_site_matvec": (C.c_int, [vp, C.c_int, ip, vp, vp, vp, vp, vp, C.c_int, vp]),
+    "sm_two_site_prepare": (C.c_int, [vp, ip, vp, vp, C.c_int, vp]),
+    "sm_two_site_matvec_prepared": (C.c_int, [vp, vp, vp, vp, vp]),
     "sm_svd": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp]),
     "sm_left_orth_2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, stp, vp,
                                      vp, ip, dp, vp]),

@@ -372,6 +372,37 @@ int sm_two_site_matvec(void* ctx, int dtype, const int* dims, const void* L, con
   return precision == SM_MATVEC_FP64 ? SM_OK : tc_status_check(c, s);
 }
 
+int sm_two_site_prepare(void* ctx, const int* dims, const void* L, const void* R, int precision,
+                        void* stream) {
+  SM_GUARD_CTX(ctx);
+  if (!dims || !L || !R) {
+    set_error("two_site_prepare: null argument");
+    return SM_ERR_VALUE;
+  }
+  for (int i = 0; i < 8; ++i)
+    if (dims[i] <= 0) {
+      set_error("two_site_prepare: non-positive dimension");
+      return SM_ERR_VALUE;
+    }
+  Ctx& c = *as_ctx(ctx);
+  return two_site_prepare(c, as_stream(stream), dims[0], dims[1], dims[2], dims[3], dims[4],
+                          dims[5], dims[6], dims[7], (const double*)L, (const double*)R,
+                          precision);
+}
+
+int sm_two_site_matvec_prepared(void* ctx, const void* H, const void* v, void* out,
+                                void* stream) {
+  SM_GUARD_CTX(ctx);
+  if (!H || !v || !out) {
+    set_error("two_site_matvec_prepared: null argument");
+    return SM_ERR_VALUE;
+  }
+  Ctx& c = *as_ctx(ctx);
+  cudaStream_t s = as_stream(stream);
+  SM_CHECK(two_site_matvec_prepared(c, s, (const double*)H, (const double*)v, (double*)out));
+  return tc_status_check(c, s);
+}
+
 int sm_ctx_set_rank_cap(void* ctx, double margin, int extra) {
   SM_GUARD_CTX(ctx);
   if (!(margin >= 1.0) || extra < 0) {

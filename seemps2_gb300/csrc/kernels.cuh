@@ -24,6 +24,21 @@ struct RankModel {
   float* b = nullptr;
 };
 
+// Prepared DMRG matvec (sm_two_site_prepare): dimensions, the caller's L and
+// R (kept alive by the caller), and their tensor-core operand planes.
+struct MatvecPrep {
+  int precision = -1;  // none prepared
+  int a = 0, c = 0, b = 0, p1 = 0, p2 = 0, e = 0, g = 0, f = 0;
+  bool tc = false;     // both products on the tensor cores (else the generic path)
+  int kpL = 0, kpR = 0;
+  const double* L = nullptr;
+  const double* R = nullptr;
+  void* Lh = nullptr;
+  float* Ll = nullptr;
+  void* Rh = nullptr;
+  float* Rl = nullptr;
+};
+
 struct Ctx {
   int device = 0;
   int num_sms = 0;
@@ -53,6 +68,7 @@ struct Ctx {
   sm_stats stats{};
   bool timing = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  MatvecPrep mvp;
   bool trace = false;
   std::vector<int> tr_rank, tr_len;
   std::vector<double> tr_err2, tr_s;
@@ -168,6 +184,12 @@ int gemm_oz(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, do
 template <typename T>
 int two_site_matvec(Ctx& ctx, cudaStream_t st, int a, int c, int b, int p1, int p2, int e, int g,
                     int f, const T* L, const T* H, const T* R, const T* v, T* out, int precision);
+// Prepared form (real, SM_MATVEC_TF32X3 / SM_MATVEC_BF16): L and R become
+// operand planes once; ctx.mvp holds them until the next prepare.
+int two_site_prepare(Ctx& ctx, cudaStream_t st, int a, int c, int b, int p1, int p2, int e,
+                     int g, int f, const double* L, const double* R, int precision);
+int two_site_matvec_prepared(Ctx& ctx, cudaStream_t st, const double* H, const double* v,
+                             double* out);
 
 // --- mps_ops.cu ------------------------------------------------------------
 template <typename T>

@@ -1,4 +1,5 @@
-"""DMRG two-site effective-Hamiltonian matvec (sm_two_site_matvec) against the oracle's
+"""DMRG two-site effective-Hamiltonian matvec (sm_two_site_matvec and the prepared
+sm_two_site_matvec_prepared) against the oracle's
 restatement of QuadraticForm.two_site_operator._matvec, at every precision, and the Lanczos
 solver against a dense eigensolver.  Bars (relative Frobenius error of the matvec): FP64 and
 FP64-accurate tensor cores 1e-13, 3xTF32 1e-5, BF16 2e-2; Lanczos lowest eigenvalue 1e-10
@@ -45,6 +46,34 @@ def test_matvec_matches_oracle(precision, dims):
     ref = do.two_site_matvec(L, H, R, v)
     rel = np.linalg.norm(out - ref) / np.linalg.norm(ref)
     assert rel < BARS[precision], rel
+
+
+@pytest.mark.parametrize("precision", ["tf32x3", "bf16"])
+@pytest.mark.parametrize("dims", [(64, 5, 64, 2, 5, 64, 64), (200, 3, 150, 2, 4, 130, 170),
+                                  (256, 5, 256, 2, 5, 256, 256), (130, 5, 100, 2, 5, 70, 90)])
+def test_prepared_matvec_matches_oracle(precision, dims):
+    """The prepared operator (environments as tensor-core planes once, FP32 X1 and MPO step) at
+    the same bars; several matvecs of one operator, and two operators alternating (each matvec
+    after the other's prepares its own planes again)."""
+    a, c, b, p, e, g, f = dims
+    rng = np.random.default_rng(sum(dims) + 1)
+    L, H, R, v = _random_block(a, c, b, p, e, g, f, rng)
+    L2, H2, R2, v2 = _random_block(a, c, b, p, e, g, f, rng)
+    op = dmrg.TwoSiteOperator(L, H, R, precision)
+    op2 = dmrg.TwoSiteOperator(L2, H2, R2, precision)
+    for _ in range(2):
+        for o, (Lx, Hx, Rx, vx) in ((op, (L, H, R, v)), (op2, (L2, H2, R2, v2))):
+            out = o.matvec(vx).cpu().numpy()
+            ref = do.two_site_matvec(Lx, Hx, Rx, vx)
+            rel = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+            assert rel < BARS[precision], rel
+
+
+def test_prepared_rejects_fp64():
+    rng = np.random.default_rng(5)
+    L, H, R, v = _random_block(64, 5, 64, 2, 5, 64, 64, rng)
+    with pytest.raises(ValueError):
+        dmrg.TwoSiteOperator(L, H, R, "fp64")
 
 
 def test_complex_matvec_fp64():
