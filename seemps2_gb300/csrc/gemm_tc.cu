@@ -462,7 +462,8 @@ int gemm_tc_planes(Ctx& ctx, cudaStream_t st, int M, int N, int kp, bool bf16, c
   const int kt_per = (ktiles + nz - 1) / nz;
   nz = (ktiles + kt_per - 1) / kt_per;
   OutT* part = nullptr;
-  if (nz > 1) SM_CHECK(ctx.scratch(sizeof(OutT) == 8 ? "tc.part" : "tc.part32", (size_t)nz * M * N, &part));
+  if (nz > 1)
+    SM_CHECK(ctx.scratch(sizeof(OutT) == 8 ? "tc.part" : "tc.part32", (size_t)nz * M * N, &part));
   const dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, nz);
   if (bf16) {
     SM_CHECK(raise_smem_limit(k_gemm_tc<true, OutT>, TcMode<true>::smem));

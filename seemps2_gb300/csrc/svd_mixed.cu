@@ -63,7 +63,8 @@ constexpr int kCW = 16;            // CTAs per cluster
 constexpr int kCNT = 512;          // threads per CTA
 constexpr int kCNW = kCNT / 32;    // warps per CTA
 constexpr int kMaxRows = 512;      // rows of R the Jacobi phase takes (32 blocks of <= 16)
-constexpr float kStopC2 = 4e-6f;   // Jacobi: a sweep whose rotations all start below cos 2e-3 ends it
+// Jacobi: a sweep whose rotations all start below cosine 2e-3 ends the iteration
+constexpr float kStopC2 = 4e-6f;
 constexpr int kQB = 8;             // widest column block of the QR (reflectors per cluster barrier)
 constexpr int kPanelRP = 2;        // rows per thread of the QR panel in registers (kw <= 1024)
 
@@ -86,7 +87,8 @@ __host__ __device__ inline size_t qr_cols_elems(int ncs, int kw) {
 template <typename F>
 __host__ __device__ inline size_t qr_bytes(int ncs, int kw, int qb) {
   const size_t kwp = (size_t)((kw + 3) & ~3);
-  const size_t slab = sizeof(F) * (size_t)(kCNW + 1) * qb * 32 + sizeof(float) * (size_t)(qb + kCNW) * 32;
+  const size_t slab =
+      sizeof(F) * (size_t)(kCNW + 1) * qb * 32 + sizeof(float) * (size_t)(qb + kCNW) * 32;
   return sizeof(F) * (qr_cols_elems<F>(ncs, kw) + 2 * kwp * qb + 2 * kQB * kQB) + slab;
 }
 
@@ -407,10 +409,6 @@ __global__ void __launch_bounds__(kCNT, 1)
   };
   auto Vpar = [&](int p) { return Vb + (size_t)p * kwp * qb; };
   auto Tpar = [&](int p) { return Tm + (size_t)p * kQB * kQB; };
-  // Panel of the owner CTA: columns cp .. cp+nbp-1 (slots sp ..), warp k owns
-  // column cp + k.  Writes the block of reflectors (rows cp.., zero above each
-  // reflector's first row) into Vpar(p), its T factor into Tpar(p), and the
-  // in-panel weights inpanel[k][i] = |R[cp+i+1 .. cp+k, cp+k]|^2 (i < k).
   // Panel of the owner CTA: columns cp .. cp+nbp-1 (slots sp ..), factored by
   // the whole CTA.  Thread t holds rows t and t + 512 of the panel's columns
   // in registers; each reflector is two CTA-wide sums (the column norm with
@@ -437,89 +435,91 @@ __global__ void __launch_bounds__(kCNT, 1)
       v0s[i] = F32<T>::zero();
       taus[i] = 0.f;
     }
-    // v_m on a row below its pivot is the column's stored value
+    // reflectors one by one (v_m on a row below its pivot is the column's
+    // stored value)
 #pragma unroll
     for (int i = 0; i < kQB; ++i) {
       if (i < nbp) {
-      const int j = cp + i;
-      // the pivot row's values: x_i[j] and v_m[j] = x_m[j] (m < i)
+        const int j = cp + i;
+        // the pivot row's values: x_i[j] and v_m[j] = x_m[j] (m < i)
 #pragma unroll
-      for (int pr = 0; pr < kPanelRP; ++pr)
-        if (tid + kCNT * pr == j) {
+        for (int pr = 0; pr < kPanelRP; ++pr)
+          if (tid + kCNT * pr == j) {
 #pragma unroll
-          for (int m = 0; m <= i; ++m) ctrl->prow[m] = make_float2(f_re(x[pr][m]), f_im(x[pr][m]));
-        }
-      // |x_i|^2 over rows >= j; sum over rows > j of conj(v_m) x_i (m < i)
-      float red[16];
+            for (int m = 0; m <= i; ++m)
+              ctrl->prow[m] = make_float2(f_re(x[pr][m]), f_im(x[pr][m]));
+          }
+        // |x_i|^2 over rows >= j; sum over rows > j of conj(v_m) x_i (m < i)
+        float red[16];
 #pragma unroll
-      for (int a = 0; a < 16; ++a) red[a] = 0.f;
+        for (int a = 0; a < 16; ++a) red[a] = 0.f;
 #pragma unroll
-      for (int pr = 0; pr < kPanelRP; ++pr) {
-        const int row = tid + kCNT * pr;
-        if (row >= j && row < kw) red[0] += f_abs2(x[pr][i]);
-        if (row > j && row < kw) {
+        for (int pr = 0; pr < kPanelRP; ++pr) {
+          const int row = tid + kCNT * pr;
+          if (row >= j && row < kw) red[0] += f_abs2(x[pr][i]);
+          if (row > j && row < kw) {
 #pragma unroll
-          for (int m = 0; m < i; ++m) {
-            float gr = 0.f, gi = 0.f;
-            f_dotc(x[pr][m], x[pr][i], gr, gi);
-            red[1 + 2 * m] += gr;
-            red[2 + 2 * m] += gi;
+            for (int m = 0; m < i; ++m) {
+              float gr = 0.f, gi = 0.f;
+              f_dotc(x[pr][m], x[pr][i], gr, gi);
+              red[1 + 2 * m] += gr;
+              red[2 + 2 * m] += gi;
+            }
           }
         }
-      }
-      cta_sum(ctrl, red, 1 + 2 * i);
-      const float2 xp = ctrl->prow[i];
-      F x0;
-      f_set(x0, xp.x, xp.y);
-      const float xn = sqrtf(red[0]);
-      const float a0 = sqrtf(f_abs2(x0));
-      float pr_ = 1.f, pi_ = 0.f;  // phase of x_j
-      if (a0 > 0.f) {
-        pr_ = f_re(x0) / a0;
-        pi_ = f_im(x0) / a0;
-      }
-      f_set(v0s[i], f_re(x0) + pr_ * xn, f_im(x0) + pi_ * xn);
-      taus[i] = xn > 0.f ? 1.0f / (xn * (xn + a0)) : 0.f;
-      // Gram entries v_m^H v_i = (rows > j) + conj(v_m[j]) v0_i
-      if (tid == 0) {
-#pragma unroll
-        for (int m = 0; m < i; ++m) {
-          const float2 vm = ctrl->prow[m];
-          const float gr = red[1 + 2 * m] + vm.x * f_re(v0s[i]) + vm.y * f_im(v0s[i]);
-          const float gi = red[2 + 2 * m] + vm.x * f_im(v0s[i]) - vm.y * f_re(v0s[i]);
-          ctrl->gram[m][i] = make_float2(gr, gi);
+        cta_sum(ctrl, red, 1 + 2 * i);
+        const float2 xp = ctrl->prow[i];
+        F x0;
+        f_set(x0, xp.x, xp.y);
+        const float xn = sqrtf(red[0]);
+        const float a0 = sqrtf(f_abs2(x0));
+        float pr_ = 1.f, pi_ = 0.f;  // phase of x_j
+        if (a0 > 0.f) {
+          pr_ = f_re(x0) / a0;
+          pi_ = f_im(x0) / a0;
         }
-      }
-      // v_i on this thread's rows; the pivot row of column i becomes -nu
-      F vi[kPanelRP];
+        f_set(v0s[i], f_re(x0) + pr_ * xn, f_im(x0) + pi_ * xn);
+        taus[i] = xn > 0.f ? 1.0f / (xn * (xn + a0)) : 0.f;
+        // Gram entries v_m^H v_i = (rows > j) + conj(v_m[j]) v0_i
+        if (tid == 0) {
 #pragma unroll
-      for (int pr = 0; pr < kPanelRP; ++pr) {
-        const int row = tid + kCNT * pr;
-        vi[pr] = (row > j && row < kw) ? x[pr][i] : (row == j ? v0s[i] : F32<T>::zero());
-        if (row == j) f_set(x[pr][i], -pr_ * xn, -pi_ * xn);
-      }
-      // d_k = v_i^H x_k (k > i), then x_k -= tau d_k v_i
-      float dd[16];
+          for (int m = 0; m < i; ++m) {
+            const float2 vm = ctrl->prow[m];
+            const float gr = red[1 + 2 * m] + vm.x * f_re(v0s[i]) + vm.y * f_im(v0s[i]);
+            const float gi = red[2 + 2 * m] + vm.x * f_im(v0s[i]) - vm.y * f_re(v0s[i]);
+            ctrl->gram[m][i] = make_float2(gr, gi);
+          }
+        }
+        // v_i on this thread's rows; the pivot row of column i becomes -nu
+        F vi[kPanelRP];
 #pragma unroll
-      for (int a = 0; a < 16; ++a) dd[a] = 0.f;
+        for (int pr = 0; pr < kPanelRP; ++pr) {
+          const int row = tid + kCNT * pr;
+          vi[pr] = (row > j && row < kw) ? x[pr][i] : (row == j ? v0s[i] : F32<T>::zero());
+          if (row == j) f_set(x[pr][i], -pr_ * xn, -pi_ * xn);
+        }
+        // d_k = v_i^H x_k (k > i), then x_k -= tau d_k v_i
+        float dd[16];
 #pragma unroll
-      for (int pr = 0; pr < kPanelRP; ++pr) {
+        for (int a = 0; a < 16; ++a) dd[a] = 0.f;
+#pragma unroll
+        for (int pr = 0; pr < kPanelRP; ++pr) {
+#pragma unroll
+          for (int k = i + 1; k < kQB; ++k) {
+            float gr = 0.f, gi = 0.f;
+            f_dotc(vi[pr], x[pr][k], gr, gi);
+            dd[2 * k] += gr;
+            dd[2 * k + 1] += gi;
+          }
+        }
+        cta_sum(ctrl, dd, 2 * nbp);
 #pragma unroll
         for (int k = i + 1; k < kQB; ++k) {
-          float gr = 0.f, gi = 0.f;
-          f_dotc(vi[pr], x[pr][k], gr, gi);
-          dd[2 * k] += gr;
-          dd[2 * k + 1] += gi;
+          const float wr = taus[i] * dd[2 * k], wi = taus[i] * dd[2 * k + 1];
+#pragma unroll
+          for (int pr = 0; pr < kPanelRP; ++pr) f_axpy(wr, wi, vi[pr], x[pr][k]);
         }
       }
-      cta_sum(ctrl, dd, 2 * nbp);
-#pragma unroll
-      for (int k = i + 1; k < kQB; ++k) {
-        const float wr = taus[i] * dd[2 * k], wi = taus[i] * dd[2 * k + 1];
-#pragma unroll
-        for (int pr = 0; pr < kPanelRP; ++pr) f_axpy(wr, wi, vi[pr], x[pr][k]);
-      }
-    }
     }
     // R entries and reflectors back to shared memory
     F* Vp = Vpar(p);
@@ -541,7 +541,8 @@ __global__ void __launch_bounds__(kCNT, 1)
         const int rr = row - cp;
         if (rr >= 1 && rr < kQB) {
 #pragma unroll
-          for (int k = 0; k < kQB; ++k) ctrl->rsq[rr][k] = (k < nbp && k >= rr) ? f_abs2(x[pr][k]) : 0.f;
+          for (int k = 0; k < kQB; ++k)
+            ctrl->rsq[rr][k] = (k < nbp && k >= rr) ? f_abs2(x[pr][k]) : 0.f;
         }
       }
     }
