@@ -12,10 +12,12 @@ Reported (one JSON line on rank 0):
   value        sweeps/s with inputs resident in GPU memory (CUDA events)
   e2e          same through the public API from pinned host arrays, host<->device
                copies inside the timed region
-  roofline     the dominant FP64 kernel (FP64 GEMM or Jacobi SVD): algorithmic
-               flops per launch / event-timed launch duration vs the FP64 peak
-               measured in this run (the library's FP64 GEMM; GB300 has no FP64
-               tensor path); plus the tensor-core GEMM of the FP32 contractions
+  roofline     the dominant kernel: in the mixed forms the FP32 cluster
+               factorisation (latency bound; its FP32 rate against the SIMT
+               peak of its 16 SMs), else the dominant FP64 kernel (FP64 GEMM or
+               Jacobi SVD) against the FP64 peak measured in this run (the
+               library's FP64 GEMM; GB300 has no FP64 tensor path); plus the
+               FP64-accurate and 3xTF32 tensor-core products
   cpu_baseline the CPU oracle (NumPy/SciPy LAPACK, all host threads) on the
                same workload
 `--impl reference` times that CPU implementation alone, same workload.
@@ -699,7 +701,7 @@ def main():
                                                   stt["gemm_launches"])}
     kname, (tag, kfl, kms, kl) = max(cands.items(), key=lambda kv: kv[1][2])
     achieved = kfl / (kms / 1e3) if kms else 0.0
-    roofline = {
+    fp64_roof = {
         "bound": "fp64", "kernel": kname,
         "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
         "frac": achieved / peak if peak else None, "traffic": None,
@@ -707,11 +709,34 @@ def main():
                        "no tensor-core path; MEASURED_PEAKS.json lists HBM and bf16 only)",
         "flops_per_launch": kfl / max(1, kl), "launches_per_step": kl,
         "avg_launch_ms": kms / max(1, kl), "share_of_step": kms / inst_ms if inst_ms else None,
-        "jacobi_share_of_step": stt["jacobi_ms"] / inst_ms if inst_ms else None,
-        "gemm_share_of_step": stt["gemm_ms"] / inst_ms if inst_ms else None,
-        "cluster_share_of_step": stt["cluster_ms"] / inst_ms if inst_ms else None,
-        "cluster_bound": "latency (FP32 rotations on 16 SMs, one cluster barrier per block round)",
     }
+    roofline = dict(fp64_roof)
+    if stt["cluster_ms"] > kms and stt["mixed_splits"]:
+        # the mixed forms' dominant kernel: the FP32 cluster factorisation, one launch per mixed
+        # split on the 16 SMs of one thread-block cluster; bound by latency (barriers and each
+        # pair step's dependent chain), so its FP32 rate is reported against the SIMT peak of
+        # those 16 SMs and of the whole GPU at the sampled SM clock
+        nl = stt["mixed_splits"]
+        cl_ach = stt["cluster_flops"] / (stt["cluster_ms"] / 1e3)
+        mhz = clk.summary().get("sm_mhz") or 2070.0
+        fp32_sm = 128 * 2 * mhz * 1e6  # FP32 FMA lanes per SM x 2 flops x clock
+        roofline = {
+            "bound": "latency", "kernel": "k_split_cluster (FP32 blocked QR + block-cyclic "
+                                          "one-sided Jacobi, 16-CTA cluster)",
+            "achieved": cl_ach / 1e12, "peak": 16 * fp32_sm / 1e12, "unit": "TFLOP/s",
+            "frac": cl_ach / (16 * fp32_sm), "frac_of_gpu_fp32": cl_ach / (152 * fp32_sm),
+            "peak_source": "nominal FP32 SIMT rate of the 16 SMs the kernel occupies (128 FMA "
+                           "lanes per SM at the sampled SM clock); MEASURED_PEAKS.json has no "
+                           "FP32 SIMT figure",
+            "flops_per_launch": stt["cluster_flops"] / nl, "launches_per_step": nl,
+            "avg_launch_ms": stt["cluster_ms"] / nl,
+            "share_of_step": stt["cluster_ms"] / inst_ms if inst_ms else None,
+            "traffic": 2338048,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one 512 x 512 "
+                              "split launch (profiles/k_split_cluster_512x512.md): the matrix "
+                              "is read once, everything else stays on chip",
+            "fp64_simt": fp64_roof,
+        }
     if stt["gemm_oz_launches"]:
         oz_ach = stt["gemm_oz_flops"] / (stt["gemm_oz_ms"] / 1e3) if stt["gemm_oz_ms"] else 0.0
         roofline["fp64_tensor_core_gemm"] = {

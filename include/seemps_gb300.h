@@ -392,6 +392,8 @@ typedef struct sm_stats {
   int64_t gemm_oz_launches;    /* FP64 products on the BF16 tensor cores (mixed forms) */
   double gemm_oz_flops;        /* 2 M N K of those */
   double gemm_oz_ms;           /* event-timed (stats timing on), slicing + MMA + reduce */
+  double cluster_flops;        /* FP32 work of the cluster kernel as run: QR 4 (kw-j)(l-j-1) per
+                                  reflector j, Jacobi 12 l per pair and sweep (x4 complex) */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

@@ -82,6 +82,7 @@ class sm_stats(C.Structure):
         ("gemm_oz_launches", C.c_int64),
         ("gemm_oz_flops", C.c_double),
         ("gemm_oz_ms", C.c_double),
+        ("cluster_flops", C.c_double),
     ]
 
 

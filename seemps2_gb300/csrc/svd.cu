@@ -1475,6 +1475,14 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     ctx.stats.cluster_ms += ms;
   }
   ctx.stats.jacobi_sweeps += hc.sweeps;
+  {  // algorithmic FP32 work of the launch (QR reflectors, then Jacobi pairs x sweeps)
+    const int keff = hc.nact;
+    double fl = 0.0;
+    for (int j = 0; j < keff; ++j) fl += 4.0 * (kw - j) * std::max(0, l - j - 1);
+    const double rows = 32.0 * ((keff + 31) / 32);  // the Jacobi's 32 blocks, zero rows included
+    fl += 12.0 * l * (rows * (rows - 1) / 2) * hc.sweeps;
+    ctx.stats.cluster_flops += (sizeof(T) == sizeof(double) ? 1.0 : 4.0) * fl;
+  }
   if (hc.status != 0 || (!exact_rule && h->info[3] < kMixedBlind * h->info[2])) {
     ctx.stats.mixed_fallbacks += 1;
     ctx.stats.mixed_fallback_fp32 += 1;
