@@ -1295,12 +1295,7 @@ __global__ void __launch_bounds__(1024) k_mixed_sort(const double* __restrict__ 
 //  * mixed_rank_block: the rank (exact weights for the relative-norm rule:
 //    s_j^2 are Rayleigh quotients of orthonormal rows), err2, status, info[2],
 //    info[3], info[7];
-//  * coupling check, info[4]: the largest state change left by the coupling
-//    between a kept row i and a dropped row j, angle |G_ij| / (lambda_i -
-//    lambda_j) (lambda = s^2) times s_i / |A|_F; its square bounds the
-//    fidelity error the split can add.  Pairs whose both values lie below the
-//    FP32 resolution (s < blind s_0) are skipped: which of two unresolved
-//    directions is kept does not matter once the kept weight is exact.
+//  * info[4] = 0 for the coupling check that k_mixed_coupling runs next.
 // Dynamic shared memory: 24 cnt bytes.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_mixed_final(const T* __restrict__ G, int cnt,
@@ -1321,14 +1316,34 @@ __global__ void __launch_bounds__(1024) k_mixed_final(const T* __restrict__ G, i
   rank_sort(keys, cnt, perm, s_sorted, ss);
   __syncthreads();
   block_prefix_sq(ss, cnt, P, red);
-  const int Dsh = mixed_rank_block(ss, P, cnt, st, exact_rule, ctl, res, info, &shD, &shBad);
+  mixed_rank_block(ss, P, cnt, st, exact_rule, ctl, res, info, &shD, &shBad);
   (void)errors;
-  const int D = Dsh;
+  (void)blind;
+  if (threadIdx.x == 0) info[4] = 0.0;
+}
+
+// Coupling check of a mixed split (after k_mixed_final), over the whole grid:
+// info[4] = the largest state change left by the coupling between a kept row
+// a and a dropped row b, angle |G_ab| / (lambda_a - lambda_b) (lambda = s^2)
+// times s_a / |A|_F; its square bounds the fidelity error the split can add.
+// Pairs whose both values lie below the FP32 resolution (s < blind s_0) are
+// skipped: which of two unresolved directions is kept does not matter once
+// the kept weight is exact.  The maximum goes into info[4] by an atomic max on
+// the bits of the non-negative double (order-independent).
+template <typename T>
+__global__ void __launch_bounds__(256) k_mixed_coupling(const T* __restrict__ G, int cnt,
+                                                        const int* __restrict__ perm,
+                                                        const double* __restrict__ ss,
+                                                        const SplitResult* __restrict__ res,
+                                                        double blind, double* info) {
+  __shared__ double red[8];
+  const int D = min(res->D, cnt);
   const double sb = blind * ss[0];
   const double rnorm = info[0] > 0.0 ? 1.0 / sqrt(info[0]) : 0.0;
   double worst = 0.0;
   const long pairs = (long)D * (cnt - D);
-  for (long e = threadIdx.x; e < pairs; e += blockDim.x) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < pairs;
+       e += (long)gridDim.x * blockDim.x) {
     const int a = (int)(e / (cnt - D)), b = D + (int)(e % (cnt - D));
     if (ss[a] < sb && ss[b] < sb) continue;
     const double gap = ss[a] * ss[a] - ss[b] * ss[b];
@@ -1339,10 +1354,12 @@ __global__ void __launch_bounds__(1024) k_mixed_final(const T* __restrict__ G, i
   for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = worst;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    double w = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) w = fmax(w, __shfl_xor_sync(0xffffffffu, w, o));
-    if (threadIdx.x == 0) info[4] = w;
+  if (threadIdx.x == 0) {
+    double w = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) w = fmax(w, red[i]);
+    if (w > 0.0)
+      atomicMax(reinterpret_cast<unsigned long long*>(info + 4),
+                (unsigned long long)__double_as_longlong(w));
   }
 }
 
@@ -1547,7 +1564,12 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   if (fin_smem > 48 * 1024) SM_CHECK(raise_smem_limit(k_mixed_final<T>, fin_smem));
   k_mixed_final<T><<<1, 1024, fin_smem, st>>>(Gb, cnt, strat, exact_rule ? 1 : 0, kMixedBlind, ctl,
                                               perm, s_sorted, errors, res, info);
-  note_launch();
+  {
+    const long maxpairs = (long)(cnt / 2) * (cnt - cnt / 2);  // D (cnt - D) at its largest
+    const int cb = (int)std::max(1L, std::min((maxpairs + 255) / 256, 4L * ctx.num_sms));
+    k_mixed_coupling<T><<<cb, 256, 0, st>>>(Gb, cnt, perm, s_sorted, res, kMixedBlind, info);
+  }
+  note_launch(2);
   SM_CUDA_CHECK(cudaGetLastError());
   SplitResult* hr = reinterpret_cast<SplitResult*>(ctx.pinned);
   SM_CUDA_CHECK(cudaMemcpyAsync(hr, res, sizeof(SplitResult), cudaMemcpyDeviceToHost, st));
