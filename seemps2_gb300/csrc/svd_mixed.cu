@@ -17,18 +17,19 @@
 //            step: every CTA applies the block's qb reflectors to its columns
 //            beyond it in compact WY form (two passes over the rows; lanes
 //            own columns and warps own rows, so every reflector-row load is a
-//            shared-memory broadcast), then the CTA owning the next block
-//            factors that block's columns (its "panel": qb reflectors, one
-//            named barrier of the panel warps each) and writes the reflector
-//            block and its T factor once to global memory; after the barrier
-//            every other CTA copies them from L2 into its shared memory (a
-//            DSMEM broadcast from one SM to 15 is bound by that SM's outgoing
-//            stores, ~5 bytes per clock).  The
-//            factorisation stops at the first step whose trailing block holds
-//            at most thr of |W|_F^2 (rank revealing), leaving keff rows of R;
-//            the trailing weights of all qb steps of a block come from the
-//            column weights after the block (the later reflectors of a block
-//            leave the weight below each earlier step unchanged).
+//            shared-memory broadcast); then the CTA owning the next block
+//            factors that block's columns (its "panel") with all its threads:
+//            each holds two rows of the panel in registers, and a reflector
+//            costs two CTA-wide sums.  The owner writes the reflector block
+//            and its T factor once to global memory; after the barrier every
+//            other CTA copies them from L2 into its shared memory (a DSMEM
+//            broadcast from one SM to 15 is bound by that SM's outgoing
+//            stores, measured at ~46 bytes per clock).  The factorisation
+//            stops at the first step whose trailing block holds at most thr
+//            of |W|_F^2 (rank revealing), leaving keff rows of R; the
+//            trailing weights of all qb steps of a block come from the column
+//            weights after the block (the later reflectors of a block leave
+//            the weight below each earlier step unchanged).
 //   phase 2  the rows of R are cut into 32 blocks of r = ceil(keff / 32) rows;
 //            CTA c holds block positions c and 31 - c in shared memory.
 //   phase 3  block-cyclic one-sided Jacobi: per sweep, the pairs inside each
