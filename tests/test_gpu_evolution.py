@@ -63,9 +63,10 @@ def _oracle(rule, mpo, x, dt, steps, st):
 
 
 RK4_OPEN = pytest.mark.xfail(
-    reason="open: the FP64 one-sided Jacobi SVD (k_jacobi) reaches its sweep cap on a split of the "
-           "five-term Runge-Kutta sum (a joined bond of ~72 with rank <= 16) and raises "
-           "LinAlgError; Euler and Euler2 (two-term sums) pass", strict=False)
+    reason="open: the FP64 one-sided Jacobi SVD (k_jacobi) builds its rotation angle in FP32, which "
+           "does not converge inside the (nearly) degenerate singular-value clusters of the "
+           "Runge-Kutta sums' splits (60-sweep cap, LinAlgError); Euler and Euler2 pass",
+    strict=False)
 
 
 @pytest.mark.parametrize("rule", ["euler", "euler2", pytest.param("runge_kutta", marks=RK4_OPEN)])
