@@ -610,8 +610,8 @@ def main():
         print(json.dumps({"profile_step": args.form, "contractions": args.contractions,
                           "launches": stt["launches"]}), flush=True)
         return
-    if args.form != "plain":
-        sg.set_precision("fp64")
+    def time_form(precision, **kw):
+        sg.set_precision(precision, **kw)
         step()
         torch.cuda.synchronize()
         pt = []
@@ -625,8 +625,15 @@ def main():
             e1.synchronize()
             pt.append(e0.elapsed_time(e1))
         psw = sg.state.last_report["sweeps"]
-        plain = {"value": psw * len(pt) / (sum(pt) / 1e3), "unit": "sweeps/s",
-                 "ms_per_step": sum(pt) / len(pt)}
+        return {"value": psw * len(pt) / (sum(pt) / 1e3), "unit": "sweeps/s",
+                "ms_per_step": sum(pt) / len(pt)}
+
+    no_predictor = None
+    if args.form != "plain":
+        plain = time_form("fp64")
+    if args.form == "mixed+learned":
+        # the same mixed form without the rank predictor: what the learned cap gains
+        no_predictor = time_form("mixed", contractions=args.contractions)
     sg.set_precision({"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed+learned"}[args.form],
                      contractions=args.contractions)
     _lib.check(_lib.load().sm_ctx_set_rank_cap(_lib.context(), args.cap_margin, args.cap_extra))
@@ -717,24 +724,32 @@ def main():
         # pair step's dependent chain), so its FP32 rate is reported against the SIMT peak of
         # those 16 SMs and of the whole GPU at the sampled SM clock
         nl = stt["mixed_splits"]
-        cl_ach = stt["cluster_flops"] / (stt["cluster_ms"] / 1e3)
+        sec = stt["cluster_ms"] / 1e3
+        alg = stt["cluster_alg_flops"] / sec  # algorithmic SVD flops (4mn^2 + 8n^3 per split)
+        run = stt["cluster_flops"] / sec      # FP32 flops as run (QR reflectors, Jacobi pairs)
         mhz = clk.summary().get("sm_mhz") or 2070.0
         fp32_sm = 128 * 2 * mhz * 1e6  # FP32 FMA lanes per SM x 2 flops x clock
+        n_sm = torch.cuda.get_device_properties(0).multi_processor_count
         roofline = {
             "bound": "latency", "kernel": "k_split_cluster (FP32 blocked QR + block-cyclic "
                                           "one-sided Jacobi, 16-CTA cluster)",
-            "achieved": cl_ach / 1e12, "peak": 16 * fp32_sm / 1e12, "unit": "TFLOP/s",
-            "frac": cl_ach / (16 * fp32_sm), "frac_of_gpu_fp32": cl_ach / (152 * fp32_sm),
-            "peak_source": "nominal FP32 SIMT rate of the 16 SMs the kernel occupies (128 FMA "
-                           "lanes per SM at the sampled SM clock); MEASURED_PEAKS.json has no "
-                           "FP32 SIMT figure",
-            "flops_per_launch": stt["cluster_flops"] / nl, "launches_per_step": nl,
+            "achieved": alg / 1e12, "peak": n_sm * fp32_sm / 1e12, "unit": "TFLOP/s",
+            "frac": alg / (n_sm * fp32_sm),
+            "work_convention": "algorithmic SVD flops 4mn^2 + 8n^3 per m x n split (m >= n), "
+                               "summed over the step's cluster launches at their real shapes",
+            "peak_source": f"nominal FP32 SIMT rate of the whole GPU ({n_sm} SMs x 128 FMA lanes "
+                           "x 2 at the sampled SM clock); MEASURED_PEAKS.json has no FP32 SIMT "
+                           "figure",
+            "flops_per_launch": stt["cluster_alg_flops"] / nl, "launches_per_step": nl,
             "avg_launch_ms": stt["cluster_ms"] / nl,
             "share_of_step": stt["cluster_ms"] / inst_ms if inst_ms else None,
-            "traffic": 2338048,
-            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one 512 x 512 "
-                              "split launch (profiles/k_split_cluster_512x512.md): the matrix "
-                              "is read once, everything else stays on chip",
+            "traffic": stt["cluster_bytes"] / nl,
+            "traffic_source": "derived per launch: the split matrix read once and the converged "
+                              "rows written (FP64); an ncu capture of a 512 x 512 launch read "
+                              "1.1x the matrix bytes, everything else stays on chip",
+            "as_run": {"achieved": run / 1e12, "unit": "TFLOP/s (FP32 work as run)",
+                       "frac_of_16_sms": run / (16 * fp32_sm),
+                       "frac_of_gpu": run / (n_sm * fp32_sm)},
             "fp64_simt": fp64_roof,
         }
     if stt["gemm_oz_launches"]:
@@ -821,6 +836,9 @@ def main():
             }
             if learned_info:
                 line["learned"] = learned_info
+            if no_predictor:
+                line["mixed_without_predictor"] = no_predictor
+                line["predictor_gain"] = value / no_predictor["value"] if no_predictor["value"] else None
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

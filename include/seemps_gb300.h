@@ -234,7 +234,11 @@ int sm_left_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int 
  * return SM_ERR_VALUE.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress), so make that first call before any stream
  * capture.  All calls share the array and it keeps the last call's contents;
- * calls that overlap on the GPU race on it, so serialise them. */
+ * calls that overlap on the GPU race on it, so serialise them.  Every call
+ * reads the kept rank back to the host, so it synchronises `stream` before it
+ * returns.  Its Jacobi stage is a cooperative multi-CTA kernel; if kernels of
+ * other streams keep its CTAs off the SMs, its bounded barrier times out and
+ * the call redoes the split with a one-CTA Jacobi (slower, same result). */
 int sm_left_orth_2site_noalloc(int dtype, const void* AA, int a, int d1, int d2, int b,
                                const sm_strategy* st, void* U, void* SV, int* D,
                                double* err, void* stream);
@@ -394,14 +398,13 @@ typedef struct sm_stats {
   double gemm_oz_ms;           /* event-timed (stats timing on), slicing + MMA + reduce */
   double cluster_flops;        /* FP32 work of the cluster kernel as run: QR 4 (kw-j)(l-j-1) per
                                   reflector j, Jacobi 12 l per pair and sweep (x4 complex) */
+  double cluster_alg_flops;    /* algorithmic SVD work of the cluster launches: 4mn^2 + 8n^3 per
+                                  m x n split (m >= n, x4 complex) */
+  double cluster_bytes;        /* algorithmic bytes of the cluster launches: the split matrix read
+                                  once and the converged rows written */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);
-
-/* Device FP64 throughput probe: runs `iters` dependent FMA chains per thread
- * over the given grid and reports elapsed milliseconds (CUDA events). */
-int sm_probe_fp64(void* ctx, int blocks, int threads, int iters, double* ms,
-                  double* flops, void* stream);
 
 #ifdef __cplusplus
 }

@@ -3,10 +3,16 @@
 # tests/golden/make_golden.py can import it and record golden vectors.
 # Recipe: out-of-tree copy, setup.py build_ext, copy the built core into src/,
 # stub h5py (only the HDF5 I/O imports it) and shim importlib.metadata.version.
-# Usage: oracle/build_reference.sh [REFERENCE_DIR] [OUT_DIR]
+# Usage: oracle/build_reference.sh REFERENCE_DIR OUT_DIR
+#   REFERENCE_DIR  a checkout of the reference SeeMPS (read only)
+#   OUT_DIR        a scratch directory outside this repository for the build
 set -euo pipefail
-REF=${1:-/root/reference}
-OUT=${2:-/tmp/seemps_ref}
+if [ $# -ne 2 ]; then
+  echo "usage: $0 REFERENCE_DIR OUT_DIR" >&2
+  exit 2
+fi
+REF=$1
+OUT=$2
 mkdir -p "$OUT"
 cp -r "$REF/src" "$REF/setup.py" "$OUT/"
 chmod -R u+w "$OUT"

@@ -83,6 +83,8 @@ class sm_stats(C.Structure):
         ("gemm_oz_flops", C.c_double),
         ("gemm_oz_ms", C.c_double),
         ("cluster_flops", C.c_double),
+        ("cluster_alg_flops", C.c_double),
+        ("cluster_bytes", C.c_double),
     ]
 
 
@@ -145,7 +147,6 @@ SIGNATURES = {
     "sm_trace_read": (C.c_int, [vp, ip, i64p, ip, ip, dp, dp]),
     "sm_stats_reset": (C.c_int, [vp, C.c_int]),
     "sm_stats_read": (C.c_int, [vp, C.POINTER(sm_stats)]),
-    "sm_probe_fp64": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, vp]),
     # rank predictor (device pointers as void*, dims as a host int array)
     "sm_mlp_param_count": (C.c_int64, [C.c_int, ip]),
     "sm_mlp_cache_count": (C.c_int64, [C.c_int, ip, C.c_int]),

@@ -707,10 +707,4 @@ int sm_stats_read(void* ctx, sm_stats* out) {
   return SM_OK;
 }
 
-int sm_probe_fp64(void* ctx, int blocks, int threads, int iters, double* ms, double* flops,
-                  void* stream) {
-  SM_GUARD_CTX(ctx);
-  return probe_fp64(as_stream(stream), blocks, threads, iters, ms, flops);
-}
-
 }  // extern "C"

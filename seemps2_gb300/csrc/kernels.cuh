@@ -212,7 +212,6 @@ int set_identity(cudaStream_t st, int k, T* X, int ldx);
 template <typename T>
 int copy_block3(cudaStream_t st, const T* src, int a, int d, int b, T* dst, int A, int B,
                 int off_a, int off_b, T w);
-int probe_fp64(cudaStream_t st, int blocks, int threads, int iters, double* ms, double* flops);
 
 // --- svd.cu ----------------------------------------------------------------
 // Exact reference truncation rule on device values s_dev[0..n) (descending).

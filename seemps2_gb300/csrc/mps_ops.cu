@@ -139,19 +139,6 @@ __global__ void k_vdot_final(int nb, const double* part, double* out) {
   }
 }
 
-// Throughput probe: independent FMA chains, 8 per thread.
-__global__ void k_probe_fp64(int iters, double seed, double* sink) {
-  double a0 = seed + threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
-  double a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
-  const double m = 0.999999, c = 1e-7;
-  for (int i = 0; i < iters; ++i) {
-    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
-    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
-  }
-  const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
-  if (s == 12345.678) sink[0] = s;  // keeps the chains alive
-}
-
 template <typename T>
 int grid_for(size_t n) {
   return (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16));
@@ -240,26 +227,6 @@ int copy_block3(cudaStream_t st, const T* src, int a, int d, int b, T* dst, int 
   return SM_OK;
 }
 
-int probe_fp64(cudaStream_t st, int blocks, int threads, int iters, double* ms, double* flops) {
-  double* sink;
-  SM_CUDA_CHECK(cudaMalloc(&sink, sizeof(double)));
-  cudaEvent_t e0, e1;
-  SM_CUDA_CHECK(cudaEventCreate(&e0));
-  SM_CUDA_CHECK(cudaEventCreate(&e1));
-  k_probe_fp64<<<blocks, threads, 0, st>>>(iters / 8 + 1, 1.0, sink);  // warm-up
-  SM_CUDA_CHECK(cudaEventRecord(e0, st));
-  k_probe_fp64<<<blocks, threads, 0, st>>>(iters, 1.0, sink);
-  SM_CUDA_CHECK(cudaEventRecord(e1, st));
-  SM_CUDA_CHECK(cudaEventSynchronize(e1));
-  float t = 0.f;
-  SM_CUDA_CHECK(cudaEventElapsedTime(&t, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaFree(sink);
-  *ms = t;
-  *flops = 2.0 * 8.0 * (double)iters * blocks * threads;
-  return SM_OK;
-}
 
 #define SM_INST(T)                                                                          \
   template int scale_matrix<T>(cudaStream_t, int, int, T, T*, int);                         \

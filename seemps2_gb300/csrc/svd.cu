@@ -23,6 +23,7 @@
 // the values) and truncated by a single thread with the reference's exact
 // comparisons and summation order (no FMA contraction).
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 
@@ -328,6 +329,13 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, int 
           // correction f = 1 - d/2 + 3d^2/8, d = c^2 + s^2 - 1 ~ 1e-7, which
           // leaves c^2 + s^2 - 1 = O(d^3): each rotation is unitary to FP64
           // rounding whatever the accuracy of the angle.
+          // An FP32 angle annihilates the overlap only to ~1e-7 of itself.
+          // Far from convergence that is harmless (the next sweep finishes
+          // the job), but once the pair's cosine |g|/sqrt(ab) is small the
+          // residual no longer shrinks quadratically, and inside a cluster
+          // of (nearly) equal singular values the iteration stalls at the
+          // FP32 level.  So the FP32 angle is only taken while the cosine is
+          // at least 1e-4; the last sweeps' few rotations use FP64.
           const int ex = (__double2hiint(a + b) >> 20) & 0x7ff;
           const double sc = __hiloint2double((2046 - ex) << 20, 0);     // 2^(1023 - ex)
           const double sc_inv = __hiloint2double(ex << 20, 0);           // 2^(ex - 1023)
@@ -336,7 +344,7 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, int 
           const float gabs_f = kCplx ? sqrtf(fmaf(grs, grs, gis * gis)) : fabsf(grs);
           double tt, c, sn;
           float zf = 0.0f;
-          const bool fp32_ok = ex > 0 && ex < 2046 && gabs_f > 1e-30f;
+          const bool fp32_ok = ex > 0 && ex < 2046 && gabs_f > 1e-30f && g2 >= 1e-8 * a * b;
           if (fp32_ok) zf = 0.5f * (bs - as) / gabs_f;
           if (fp32_ok && fabsf(zf) < 1e18f) {
             const float az = fabsf(zf);
@@ -1498,7 +1506,13 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     for (int j = 0; j < keff; ++j) fl += 4.0 * (kw - j) * std::max(0, l - j - 1);
     const double rows = 32.0 * ((keff + 31) / 32);  // the Jacobi's 32 blocks, zero rows included
     fl += 12.0 * l * (rows * (rows - 1) / 2) * hc.sweeps;
-    ctx.stats.cluster_flops += (sizeof(T) == sizeof(double) ? 1.0 : 4.0) * fl;
+    const double cf = sizeof(T) == sizeof(double) ? 1.0 : 4.0;
+    ctx.stats.cluster_flops += cf * fl;
+    // the split's algorithmic SVD work, 4 m n^2 + 8 n^3 (m >= n), and its
+    // algorithmic bytes: the matrix read once, the converged rows written
+    const double mm = std::max(m, n), nn = std::min(m, n);
+    ctx.stats.cluster_alg_flops += cf * (4.0 * mm * nn * nn + 8.0 * nn * nn * nn);
+    ctx.stats.cluster_bytes += (double)sizeof(T) * ((double)m * n + (double)keff * l);
   }
   if (hc.status != 0 || (!exact_rule && h->info[3] < kMixedBlind * h->info[2])) {
     ctx.stats.mixed_fallbacks += 1;
@@ -1842,7 +1856,12 @@ constexpr size_t kNoAllocRowsBytes =
 constexpr size_t kNoAllocVecBytes = 16 * 1024;                     // norms, order, control
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocRowsBytes + kNoAllocVecBytes];
 
-static unsigned char* g_noalloc_ptr[64];  // host copies of the array's device address, per device
+// Host copies of the array's device address, one per device.  Several host
+// threads may make their first call at once: each looks the address up and
+// stores the same value, so a relaxed atomic is enough.  The address is kept
+// for the life of the process; a cudaDeviceReset (which unloads this module
+// from the device) is not supported between calls.
+static std::atomic<unsigned char*> g_noalloc_ptr[64];
 
 // One-time set-up per device (with that device current): the array's name is
 // only a host-side stand-in, the kernels need its device address.
@@ -1853,28 +1872,32 @@ static int noalloc_scratch(unsigned char** out) {
     set_error("noalloc: device ordinal out of range");
     return SM_ERR_VALUE;
   }
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    SM_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_ptr[dev] = reinterpret_cast<unsigned char*>(p);
+  unsigned char* p = g_noalloc_ptr[dev].load(std::memory_order_relaxed);
+  if (!p) {
+    void* q = nullptr;
+    SM_CUDA_CHECK(cudaGetSymbolAddress(&q, g_noalloc_scratch));
+    p = reinterpret_cast<unsigned char*>(q);
+    g_noalloc_ptr[dev].store(p, std::memory_order_relaxed);
   }
-  *out = g_noalloc_ptr[dev];
+  *out = p;
   return SM_OK;
 }
 
 // Cooperative Jacobi launch without any cache (the context-based launcher
 // keeps occupancy results in a map; this one queries the runtime each time).
+// `one_cta` runs the Jacobi as a single CTA (no inter-CTA barrier).
 template <typename T, int E>
 int launch_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
                           double defl_rel, double defl_abs, double* nrm, const double* nrm0,
-                          int* act, JacobiCtl* ctl) {
+                          int* act, JacobiCtl* ctl, bool one_cta) {
   const int npairs = (k + (k & 1)) / 2;
   int dev = 0, sms = 1, per_sm = 1;
   SM_CUDA_CHECK(cudaGetDevice(&dev));
   SM_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   auto fn = k_jacobi<T, kJacobiNT, E>;
   SM_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kJacobiNT, 0));
-  const int grid = std::max(1, std::min(npairs, std::max(1, per_sm) * std::max(1, sms)));
+  const int grid =
+      one_cta ? 1 : std::max(1, std::min(npairs, std::max(1, per_sm) * std::max(1, sms)));
   int ms = kMaxSweeps;
   int L = l + k;
   void* args[] = {&Wx, &ld, &k, &l, &L, &tol2, &use_floor, &defl_rel, &defl_abs, &ms, &nrm,
@@ -1887,32 +1910,24 @@ int launch_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double t
 template <typename T>
 int run_jacobi_noalloc(cudaStream_t st, T* Wx, int ld, int k, int l, double tol2, int use_floor,
                        double defl_rel, double defl_abs, double* nrm, const double* nrm0, int* act,
-                       JacobiCtl* ctl) {
+                       JacobiCtl* ctl, bool one_cta) {
   // k <= 256 and l <= 256 here, so a thread holds at most 4 elements per row
   const int need = (l + k + kJacobiNT - 1) / kJacobiNT;
   if (need <= 1)
     return launch_jacobi_noalloc<T, 1>(st, Wx, ld, k, l, tol2, use_floor, defl_rel, defl_abs, nrm,
-                                       nrm0, act, ctl);
+                                       nrm0, act, ctl, one_cta);
   if (need <= 2)
     return launch_jacobi_noalloc<T, 2>(st, Wx, ld, k, l, tol2, use_floor, defl_rel, defl_abs, nrm,
-                                       nrm0, act, ctl);
+                                       nrm0, act, ctl, one_cta);
   return launch_jacobi_noalloc<T, 4>(st, Wx, ld, k, l, tol2, use_floor, defl_rel, defl_abs, nrm,
-                                     nrm0, act, ctl);
+                                     nrm0, act, ctl, one_cta);
 }
 
+// One attempt at the split, from the input onwards.  `one_cta` runs the
+// Jacobi as a single CTA.
 template <typename T>
-int left_orth_2site_noalloc(cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
-                            T* left, T* right, int* D_out, double* err_out) {
-  if (m <= 0 || n <= 0) {
-    set_error("noalloc split: empty matrix");
-    return SM_ERR_VALUE;
-  }
-  if (m > kNoAllocMaxDim || n > kNoAllocMaxDim) {
-    set_error("noalloc split: matrix " + std::to_string(m) + " x " + std::to_string(n) +
-              " exceeds the static scratch limit of " + std::to_string(kNoAllocMaxDim) +
-              " per dimension");
-    return SM_ERR_VALUE;
-  }
+int noalloc_attempt(cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat, T* left,
+                    T* right, int* D_out, double* err_out, bool one_cta) {
   unsigned char* base;
   SM_CHECK(noalloc_scratch(&base));
   const int k = std::min(m, n), l = std::max(m, n);
@@ -1958,7 +1973,7 @@ int left_orth_2site_noalloc(cudaStream_t st, const T* A, int m, int n, const sm_
     double drel, dabs;
     deflation(strat, k, &drel, &dabs);
     SM_CHECK(run_jacobi_noalloc<T>(st, Wx, ld, k, l, tol * tol, use_floor ? 1 : 0, drel, dabs, nrm,
-                                   nrm0, act, ctl));
+                                   nrm0, act, ctl, one_cta));
   }
   k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
   note_launch();
@@ -1987,6 +2002,29 @@ int left_orth_2site_noalloc(cudaStream_t st, const T* A, int m, int n, const sm_
   return SM_OK;
 }
 
+template <typename T>
+int left_orth_2site_noalloc(cudaStream_t st, const T* A, long long m, long long n,
+                            const sm_strategy& strat, T* left, T* right, int* D_out,
+                            double* err_out) {
+  if (m <= 0 || n <= 0) {
+    set_error("noalloc split: empty matrix");
+    return SM_ERR_VALUE;
+  }
+  if (m > kNoAllocMaxDim || n > kNoAllocMaxDim) {
+    set_error("noalloc split: matrix " + std::to_string(m) + " x " + std::to_string(n) +
+              " exceeds the static scratch limit of " + std::to_string(kNoAllocMaxDim) +
+              " per dimension");
+    return SM_ERR_VALUE;
+  }
+  // The multi-CTA Jacobi needs all its CTAs resident at once; when kernels of
+  // other streams hold the SMs its bounded grid barrier gives up with a
+  // timeout.  The split is then redone from the input with a one-CTA Jacobi.
+  int rc = noalloc_attempt<T>(st, A, (int)m, (int)n, strat, left, right, D_out, err_out, false);
+  if (rc == SM_ERR_TIMEOUT)
+    rc = noalloc_attempt<T>(st, A, (int)m, (int)n, strat, left, right, D_out, err_out, true);
+  return rc;
+}
+
 }  // namespace sm
 
 extern "C" int sm_left_orth_2site_noalloc(int dtype, const void* AA, int a, int d1, int d2, int b,
@@ -2007,12 +2045,14 @@ extern "C" int sm_left_orth_2site_noalloc(int dtype, const void* AA, int a, int 
     return SM_ERR_VALUE;
   }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  // the products in 64 bits, so that no overflow gets past the size limit
+  const long long m = (long long)a * d1, n = (long long)d2 * b;
   if (dtype == SM_FLOAT64)
-    return left_orth_2site_noalloc<double>(s, (const double*)AA, a * d1, d2 * b, *st, (double*)U,
+    return left_orth_2site_noalloc<double>(s, (const double*)AA, m, n, *st, (double*)U,
                                            (double*)SV, D, err);
   if (dtype == SM_COMPLEX128)
-    return left_orth_2site_noalloc<cplx>(s, (const cplx*)AA, a * d1, d2 * b, *st, (cplx*)U,
-                                         (cplx*)SV, D, err);
+    return left_orth_2site_noalloc<cplx>(s, (const cplx*)AA, m, n, *st, (cplx*)U, (cplx*)SV, D,
+                                         err);
   set_error("dtype must be SM_FLOAT64 or SM_COMPLEX128");
   return SM_ERR_VALUE;
 }

@@ -62,14 +62,7 @@ def _oracle(rule, mpo, x, dt, steps, st):
     return x
 
 
-RK4_OPEN = pytest.mark.xfail(
-    reason="open: the FP64 one-sided Jacobi SVD (k_jacobi) builds its rotation angle in FP32, which "
-           "does not converge inside the (nearly) degenerate singular-value clusters of the "
-           "Runge-Kutta sums' splits (60-sweep cap, LinAlgError); Euler and Euler2 pass",
-    strict=False)
-
-
-@pytest.mark.parametrize("rule", ["euler", "euler2", pytest.param("runge_kutta", marks=RK4_OPEN)])
+@pytest.mark.parametrize("rule", ["euler", "euler2", "runge_kutta"])
 def test_stepper_matches_oracle(rule):
     psi, mpo, ost, gst = _setup()
     dt, steps = 0.01, 2

@@ -86,6 +86,77 @@ def test_svd_against_lapack(shape, cplx):
     assert np.allclose(V @ V.conj().T, np.eye(k), atol=1e-11)
 
 
+def _clustered_matrix(m, n, cplx, spectrum, rng):
+    """Q1 diag(s) Q2^H with random orthonormal Q1, Q2 and the given leading singular
+    values (the rest decays geometrically from the last one)."""
+    k = min(m, n)
+    s = np.array(spectrum[:k], dtype=np.float64)
+    if s.size < k:
+        s = np.concatenate([s, s[-1] * np.exp(-0.7 * np.arange(1, k - s.size + 1))])
+    def q(r):
+        x = rng.normal(size=(r, k))
+        if cplx:
+            x = x + 1j * rng.normal(size=(r, k))
+        return np.linalg.qr(x)[0]
+    return (q(m) * s) @ q(n).conj().T
+
+
+def _spectra(rng):
+    r5 = np.sqrt(5.0)
+    return {
+        # a threefold exact cluster, as the Laplacian's symmetry produces (sqrt 5)
+        "threefold": [3.0, r5, r5, r5, 2.0, 1.0, 0.5],
+        # several exactly repeated blocks
+        "blocks": [1.0] * 8 + [0.5] * 8 + [0.25] * 4,
+        # near-degenerate clusters: relative spread 1e-9 inside each
+        "near": sorted((c * (1.0 + 1e-9 * rng.random()) for c in (1.0, 0.3, 0.01)
+                        for _ in range(5)), reverse=True),
+        # a cluster sitting at a truncation cut of tolerance 1e-12
+        "at_cut": [1.0, 0.5, 0.5, 0.5] + [1e-7] * 6,
+    }
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("shape", [(12, 12), (40, 24), (24, 40), (64, 64), (130, 100), (256, 128)])
+def test_svd_converges_on_degenerate_spectra(shape, cplx):
+    """The FP64 Jacobi converges inside exactly and nearly degenerate clusters (it formerly
+    stalled there with an FP32 rotation angle), with singular values within 1e-12 s_max of
+    LAPACK's and an orthonormal reconstruction."""
+    rng = np.random.default_rng(hash((shape, cplx)) % (1 << 32))
+    for name, spec in _spectra(rng).items():
+        A = _clustered_matrix(*shape, cplx, spec, rng)
+        U, s, V = (to_np(x) for x in sg._destructive_svd(A))
+        _, s_ref, _ = so.svd(A)
+        sv_close(s, s_ref, 1e-12)
+        k = min(shape)
+        assert np.allclose((U * s) @ V, A, atol=1e-12 * s_ref[0]), name
+        assert np.allclose(U.conj().T @ U, np.eye(k), atol=1e-11), name
+        assert np.allclose(V @ V.conj().T, np.eye(k), atol=1e-11), name
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_two_site_splits_on_degenerate_spectra_keep_reference_ranks(cplx):
+    """Two-site splits (QR preconditioner + FP64 Jacobi) of clustered matrices: identical kept
+    rank and discarded weight to the oracle's, under the relative-norm rule at 1e-12 and 1e-8."""
+    rng = np.random.default_rng(4242 + cplx)
+    for tol in (1e-12, 1e-8):
+        st = sg.DEFAULT_STRATEGY.replace(tolerance=tol, max_bond_dimension=256)
+        ost = so.DEFAULT_STRATEGY.replace(tolerance=tol, max_bond_dimension=256)
+        for (a, b) in [(6, 6), (20, 12), (64, 64), (100, 64)]:
+            for name, spec in _spectra(rng).items():
+                AA = _clustered_matrix(2 * a, 2 * b, cplx, spec, rng).reshape(a, 2, 2, b)
+                for gpu_fn, ora_fn in [(sg._left_orth_2site, so.left_orth_2site),
+                                       (sg._right_orth_2site, so.right_orth_2site)]:
+                    L, R, e = gpu_fn(AA, st)
+                    Lo, Ro, eo = ora_fn(AA, ost)
+                    assert L.shape == Lo.shape and R.shape == Ro.shape, (name, a, b, tol)
+                    D = L.shape[-1]
+                    rec = to_np(L).reshape(-1, D) @ to_np(R).reshape(D, -1)
+                    reco = Lo.reshape(-1, D) @ Ro.reshape(D, -1)
+                    assert np.allclose(rec, reco, atol=1e-11 * np.abs(AA).max()), (name, a, b)
+                    assert abs(e - eo) <= 1e-9 * max(1e-2, eo), (name, a, b, e, eo)
+
+
 @pytest.mark.parametrize("cplx", [False, True])
 def test_two_site_splits_match_oracle(cplx):
     st = sg.DEFAULT_STRATEGY.replace(tolerance=1e-8, max_bond_dimension=20)
