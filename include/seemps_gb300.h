@@ -247,6 +247,26 @@ int sm_right_orth_2site(void* ctx, int dtype, const void* AA, int a, int d1, int
                         int b, const sm_strategy* st, void* US, void* V, int* D,
                         double* err, void* stream);
 
+/* update_left_mpo_environment (state/environments.py:19-30): out[d, e, f] =
+ * sum conj(A[a, j, d]) rho[a, c, b] O[c, j, i, e] B[b, i, f] with the bra site A
+ * (a, j, d), the MPO site O (c, j, i, e), the ket site B (b, i, f) and rho
+ * (a, c, b). */
+int sm_update_left_mpo_environment(void* ctx, int dtype, const void* rho, const void* A, int a,
+                                   int j, int d, const void* O, int c, int i, int e,
+                                   const void* B, int b, int f, void* out, void* stream);
+/* update_right_mpo_environment (state/environments.py:33-42): out[a, c, b] =
+ * sum conj(A[a, j, d]) rho[d, e, f] O[c, j, i, e] B[b, i, f] (shapes as above,
+ * rho (d, e, f)). */
+int sm_update_right_mpo_environment(void* ctx, int dtype, const void* rho, const void* A, int a,
+                                    int j, int d, const void* O, int c, int i, int e,
+                                    const void* B, int b, int f, void* out, void* stream);
+
+/* One site of MPOList.join (operators/mpo.py:679-711) for two MPOs, A applied
+ * first and B after it: C[(a c), i, k, (b d)] = sum_j B[a, i, j, b] A[c, j, k, d]
+ * with B (a, i, j, b), A (c, j, k, d) and C (a*c, i, k, b*d). */
+int sm_mpo_join(void* ctx, int dtype, const void* B, int a, int i, int j, int b, const void* A,
+                int c, int k, int d, void* C, void* stream);
+
 /* _update_left_environment (cython/environments.pxi:10-37):
  * out[n,k] = sum conj(B[l,j,n]) rho[l,i] A[i,j,k]; B is (l,j,n), A is (i,j,k). */
 int sm_update_left_environment(void* ctx, int dtype, const void* B, int l, int j,
@@ -276,6 +296,54 @@ int sm_canonicalize(void* ctx, int dtype, int L, const int* phys, int* bonds,
                     void* const* sites, const int64_t* cap, int center,
                     const sm_strategy* st, double* err, void* stream);
 
+/* _recanonicalize (cython/schmidt.pxi:96-106) in place: moves the centre from
+ * oldcenter to newcenter one site at a time with the truncated SVD updates of
+ * _update_in_canonical_form_*; same buffer rules as sm_canonicalize. */
+int sm_recanonicalize(void* ctx, int dtype, int L, const int* phys, int* bonds,
+                      void* const* sites, const int64_t* cap, int oldcenter, int newcenter,
+                      const sm_strategy* st, double* err, void* stream);
+
+/* __update_in_canonical_form_right (cython/schmidt.pxi:18-42, the body of
+ * _update_in_canonical_form_right :45-56): SVD of A (a*i x b), truncation,
+ * U -> U_out (a, i, D) and (s V) @ next -> next_out (D, j, c), where next is the
+ * following site (b, j, c).  U_out holds a*i*min(a*i, b) elements, next_out
+ * min(a*i, b)*j*c.  *err = sqrt(discarded weight). */
+int sm_update_in_canonical_form_right(void* ctx, int dtype, const void* A, int a, int i,
+                                      int b, const void* next, int j, int c,
+                                      const sm_strategy* st, void* U_out, void* next_out,
+                                      int* D, double* err, void* stream);
+/* __update_in_canonical_form_left (cython/schmidt.pxi:59-82, body of
+ * _update_in_canonical_form_left :84-93): SVD of A (a x i*b), truncation,
+ * V -> V_out (D, i, b) and prev @ (U s) -> prev_out (p, j, D), where prev is the
+ * preceding site (p, j, a).  V_out holds min(a, i*b)*i*b elements, prev_out
+ * p*j*min(a, i*b). */
+int sm_update_in_canonical_form_left(void* ctx, int dtype, const void* A, int a, int i, int b,
+                                     const void* prev, int p, int j, const sm_strategy* st,
+                                     void* V_out, void* prev_out, int* D, double* err,
+                                     void* stream);
+
+/* _contract_nrjl_ijk_klm (cython/contractions.pxi:102-127):
+ * out[i, n, r, m] = sum U[(n r), (j l)] A[i, j, k] B[k, l, m] with A (a, d, b),
+ * B (b, e, c) and U (nr x d*e), nr = d*e; out is (a, d, e, c). */
+int sm_contract_nrjl_ijk_klm(void* ctx, int dtype, const void* U, int nr, const void* A,
+                             int a, int d, int b, const void* B, int e, int c, void* out,
+                             void* stream);
+
+/* AntilinearForm.tensor2site (state/antilinear.py:68-98): out[l, d1, d2, r] =
+ * sum L[l, i] A[i, d1, k] B[k, d2, n] R[n, r] for the environments L (l x i),
+ * R (n x r) and the ket sites A (i, d1, k), B (k, d2, n). */
+int sm_tensor2site(void* ctx, int dtype, const void* L, int l, int i, const void* A, int d1,
+                   int k, const void* B, int d2, int n, const void* R, int r, void* out,
+                   void* stream);
+
+/* _select_svd_driver (cython/svd.pxi:25-32): "gesdd" or "gesvd", else
+ * SM_ERR_VALUE.  The reference picks a LAPACK driver; the device has one SVD
+ * (QR-preconditioned one-sided Jacobi) whose singular values and kept ranks
+ * agree with either driver's, so the choice is recorded (sm_svd_driver: 0 =
+ * gesdd, 1 = gesvd) and changes no result. */
+int sm_select_svd_driver(const char* name);
+int sm_svd_driver(void);
+
 /* simplify / simplify_mps_sum (state/simplification.py:32-280) of
  * sum_t w_t |psi_t> (nterms >= 1; weights as (re, im) pairs).  ket_bonds holds
  * nterms*(L+1) ints, ket_sites nterms*L pointers, term_errors the nterms
@@ -303,6 +371,22 @@ int sm_simplify_gram(void* ctx, int dtype, int L, const int* phys, int nterms,
                      const double* gram, const sm_strategy* st, int direction,
                      void* const* out_sites, const int64_t* out_cap, int* out_bonds,
                      sm_simplify_report* rep, void* stream);
+
+/* sm_simplify (gram may be null, else as for sm_simplify_gram) starting the
+ * variational sweeps from a caller's guess instead of the joined kets: the
+ * `guess` argument of simplify / simplify_mps_sum (state/simplification.py:
+ * 36,93-98 and :150-155,214-219).  The guess (bonds guess_bonds (L+1), sites
+ * guess_sites) is copied and brought to canonical form at the start site with
+ * the strategy's truncation, as CanonicalMPS(guess, center=start) does; the
+ * caller's buffers are not modified.  out_cap must also cover the guess's
+ * bonds.  Only the variational methods use the guess (as in the reference). */
+int sm_simplify_guess(void* ctx, int dtype, int L, const int* phys, int nterms,
+                      const double* weights, const int* ket_bonds,
+                      const void* const* ket_sites, const double* term_errors,
+                      const double* gram, const int* guess_bonds,
+                      const void* const* guess_sites, const sm_strategy* st, int direction,
+                      void* const* out_sites, const int64_t* out_cap, int* out_bonds,
+                      sm_simplify_report* rep, void* stream);
 
 /* <O bra|O ket> for an MPO O (site i: mpo_bonds[i] x dout[i] x din[i] x
  * mpo_bonds[i+1]) and two MPS with physical dimensions din: the scprod

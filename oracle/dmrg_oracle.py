@@ -91,3 +91,93 @@ def heisenberg_mpo(n: int, J: float = 1.0):
     W[3, :, :, 4] = J * Sz
     W[4, :, :, 4] = I2
     return [W[:1]] + [W] * (n - 2) + [W[:, :, :, 4:]]
+
+
+# ---------------------------------------------------------------------------
+# The two-site DMRG driver (optimization/dmrg.py:15-199) with scipy's eigsh, as the
+# reference runs it; uses the MPS oracle's canonical forms and two-site splits.
+# ---------------------------------------------------------------------------
+
+
+def mpo_expectation(W, state, center):
+    """<state|W|state> (operators/mpo.py:378-416) for a state in canonical form about center."""
+    left = right = begin_mpo_environment()
+    for i in range(0, center):
+        left = update_left_mpo_environment(left, state[i], W[i], state[i])
+    for i in range(len(W) - 1, center - 1, -1):
+        right = update_right_mpo_environment(right, state[i], W[i], state[i])
+    return np.dot(left.reshape(-1), right.reshape(-1))
+
+
+def _energy_and_variance(W, state, center):
+    """optimization/dmrg.py:56-60: <H> and |<H psi|H psi> - <H>^2|."""
+    from oracle import seemps_oracle as so
+
+    energy = mpo_expectation(W, state, center).real
+    hpsi = [so.mpo_multiply_tensor(O, A) for O, A in zip(W, state)]
+    return energy, abs(so.norm_squared(hpsi) - energy * energy)
+
+
+def dmrg(W, guess, maxiter=20, tol=1e-10, tol_up=None, tol_eigs=None, strategy=None):
+    """optimization/dmrg.py:76-199 on lists of tensors: guess canonicalised at site 0 and
+    normalised, sweeps of eigsh(which="SA") on the two-site operators from the current
+    two-site tensor, left/right splits with the strategy (normalize=True), energy and
+    variance after each sweep, the same stop rule.  Returns (best energy, best state,
+    trajectory, variances, converged, sweeps)."""
+    import scipy.sparse.linalg as sla
+
+    from oracle import seemps_oracle as so
+
+    tol_up = tol if tol_up is None else tol_up
+    tol_eigs = tol if tol_eigs is None else tol_eigs
+    strat = (so.DEFAULT_STRATEGY if strategy is None else strategy).replace(normalize=True)
+    size = len(W)
+    state, center, _ = so.canonical_mps([np.array(A) for A in guess], 0, strat)
+    state[center] = state[center] / np.linalg.norm(state[center])
+    # environments: right ones for the first sweep (quadratic.py:40-76)
+    left = [begin_mpo_environment()] * size
+    right = [begin_mpo_environment()] * size
+    env = right[-1]
+    for i in range(size - 1, 0, -1):
+        right[i - 1] = env = update_right_mpo_environment(env, state[i], W[i], state[i])
+    energy, variance = _energy_and_variance(W, state, center)
+    best = (energy, [A.copy() for A in state])
+    trajectory, variances = [energy], [variance]
+    direction, last_energy, converged, sweeps = +1, energy, False, 0
+    for sweep in range(1, maxiter + 1):
+        sweeps = sweep
+        sites = range(size - 1) if direction > 0 else range(size - 2, -1, -1)
+        for i in sites:
+            L, R = left[i], right[i + 1]
+            H = two_site_hamiltonian(W[i], W[i + 1])
+            v = np.tensordot(state[i], state[i + 1], axes=1)
+            n = v.size
+            op = sla.LinearOperator((n, n), matvec=lambda x, L=L, H=H, R=R, s=v.shape:
+                                    two_site_matvec(L, H, R, x.reshape(s)).reshape(-1),
+                                    dtype=np.float64)
+            _, evec = sla.eigsh(op, 1, which="SA", v0=v.reshape(-1), tol=tol_eigs)
+            AB = evec.reshape(v.shape)
+            if direction > 0:
+                state[i], state[i + 1], _ = so.left_orth_2site(AB, strat)
+                center = i + 1
+                if i < size - 2:
+                    left[i + 1] = update_left_mpo_environment(left[i], state[i], W[i], state[i])
+            else:
+                state[i], state[i + 1], _ = so.right_orth_2site(AB, strat)
+                center = i
+                if i > 0:
+                    right[i] = update_right_mpo_environment(right[i + 1], state[i + 1],
+                                                            W[i + 1], state[i + 1])
+        direction = -direction
+        energy, variance = _energy_and_variance(W, state, center)
+        trajectory.append(energy)
+        variances.append(variance)
+        if energy < best[0]:
+            best = (energy, [A.copy() for A in state])
+        change = energy - last_energy
+        scale = max(1.0, abs(energy))
+        if change > tol_up * scale or -tol * scale <= change <= 0:
+            converged = True
+            break
+        last_energy = energy
+    return best[0], best[1], trajectory, variances, converged, sweeps

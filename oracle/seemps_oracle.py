@@ -561,8 +561,10 @@ def simplify_mps_sum(
     direction: int = +1,
     errors: list | None = None,
     rec: Recorder | None = None,
+    guess: list | None = None,
 ) -> SimplifyResult:
-    """Variational simplification of sum_i w_i psi_i (simplification.py:150-280)."""
+    """Variational simplification of sum_i w_i psi_i (simplification.py:150-280); a guess
+    replaces the joined sum as the starting state (:214-219)."""
     norm_state_sqr, weights, states = mpssum_norm_squared(weights, states)
     if errors is None:
         errors = [0.0] * len(states)
@@ -571,7 +573,8 @@ def simplify_mps_sum(
         return SimplifyResult(zero, 0, 0.0)
     start = 0 if direction > 0 else -1
     mps, center, _ = canonical_mps(
-        mpssum_join(weights, states), start, strategy, normalize=False, rec=rec
+        mpssum_join(weights, states) if guess is None else guess, start, strategy,
+        normalize=False, rec=rec
     )
     size = len(mps)
     forms = [AntilinearForm(mps, si, center=center) for si in states]
@@ -611,6 +614,44 @@ def simplify_mps_sum(
         mps[center] = last / factor
         total_error_bound /= factor
     return SimplifyResult(mps, center, total_error_bound, sweeps, errs, norm_state_sqr)
+
+
+def contract_nrjl_ijk_klm(U, A, B):
+    """np.einsum('ijk,klm,nrjl -> inrm', A, B, U) (cython/contractions.pxi:102-127)."""
+    a, d, b = A.shape
+    _, e, c = B.shape
+    AB = (A.reshape(a * d, b) @ B.reshape(b, e * c)).reshape(a, d * e, c)
+    return np.matmul(U, AB).reshape(a, d, e, c)
+
+
+def mpo_join(mpos: list) -> list:
+    """MPOList.join (operators/mpo.py:679-711): per site, the tensors joined from the last
+    MPO backwards, aijb,cjkd->acikbd with the later MPO's tensor first."""
+    out = []
+    for s in range(len(mpos[0])):
+        ts = [m[s] for m in mpos]
+
+        def join(A, *args):
+            if not args:
+                return A
+            B = join(*args)
+            a, d, _, b = A.shape
+            c, _, _, e = B.shape
+            aux = np.tensordot(B, A, ((2,), (1,)))
+            return np.ascontiguousarray(aux.transpose(0, 3, 1, 4, 2, 5).reshape(a * c, d, d, b * e))
+
+        out.append(join(*ts))
+    return out
+
+
+def simplify_mpo(mpo: list, strategy: Strategy, direction: int = +1, guess: list | None = None):
+    """simplify_mpo (operators/simplify_mpo.py:50-89) on a list of MPO tensors: as an MPS of
+    physical dimension i*j, simplified, and back."""
+    as_mps = [O.reshape(O.shape[0], O.shape[1] * O.shape[2], O.shape[3]) for O in mpo]
+    g = None if guess is None else [O.reshape(O.shape[0], -1, O.shape[3]) for O in guess]
+    res = simplify(as_mps, strategy, direction, guess=g)
+    s = int(round(np.sqrt(mpo[0].shape[1] * mpo[0].shape[2])))
+    return [A.reshape(A.shape[0], s, s, A.shape[2]) for A in res.tensors], res
 
 
 def mpo_apply(

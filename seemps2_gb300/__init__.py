@@ -16,20 +16,32 @@ from .core import (
     Simplification,
     Strategy,
     Truncation,
+    _begin_environment,
+    _canonicalize,
     _contract_last_and_first,
+    _contract_nrjl_ijk_klm,
     _destructive_svd,
+    _end_environment,
     _gemm,
+    _join_environments,
     _left_orth_2site,
     _mpo_multiply_tensor,
+    _recanonicalize,
     _right_orth_2site,
+    _select_svd_driver,
+    _tensor2site,
+    _update_in_canonical_form_left,
+    _update_in_canonical_form_right,
     _update_left_environment,
     _update_right_environment,
     destructively_truncate_vector,
 )
 from ._lib import set_precision
-from .operators import MPO, MPOList, mpo_scprod
+from .operators import (CANONICALIZE_MPO, MPO, MPO_SIMPLIFICATION_STRATEGY, MPOList,
+                        mpo_as_mps, mpo_scprod, mps_as_mpo, simplify_mpo)
 from .state import (
     SIMPLIFICATION_STRATEGY,
+    AntilinearForm,
     CanonicalMPS,
     MPS,
     MPSSum,
@@ -47,4 +59,6 @@ __all__ = [
     "Simplification", "Strategy", "Truncation", "destructively_truncate_vector", "MPO", "MPOList",
     "SIMPLIFICATION_STRATEGY", "CanonicalMPS", "MPS", "MPSSum", "random_mps", "random_uniform_mps",
     "scprod", "simplify", "simplify_mps", "simplify_mps_sum", "vdot", "set_precision", "mpo_scprod",
+    "AntilinearForm", "simplify_mpo", "mpo_as_mps", "mps_as_mpo", "MPO_SIMPLIFICATION_STRATEGY",
+    "CANONICALIZE_MPO",
 ]

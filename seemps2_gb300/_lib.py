@@ -135,6 +135,29 @@ SIGNATURES = {
     "sm_scprod": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(vp), ip, C.POINTER(vp), dp, vp]),
     "sm_canonicalize": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(vp), i64p, C.c_int, stp,
                                   dp, vp]),
+    "sm_recanonicalize": (C.c_int, [vp, C.c_int, C.c_int, ip, ip, C.POINTER(vp), i64p, C.c_int,
+                                    C.c_int, stp, dp, vp]),
+    "sm_update_in_canonical_form_right": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp,
+                                                    C.c_int, C.c_int, stp, vp, vp, ip, dp, vp]),
+    "sm_update_in_canonical_form_left": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp,
+                                                   C.c_int, C.c_int, stp, vp, vp, ip, dp, vp]),
+    "sm_contract_nrjl_ijk_klm": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int,
+                                           vp, C.c_int, C.c_int, vp, vp]),
+    "sm_update_left_mpo_environment": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, vp,
+                                                 C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int,
+                                                 vp, vp]),
+    "sm_update_right_mpo_environment": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int,
+                                                  vp, C.c_int, C.c_int, C.c_int, vp, C.c_int,
+                                                  C.c_int, vp, vp]),
+    "sm_mpo_join": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int,
+                              C.c_int, C.c_int, vp, vp]),
+    "sm_tensor2site": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp,
+                                 C.c_int, C.c_int, vp, C.c_int, vp, vp]),
+    "sm_select_svd_driver": (C.c_int, [C.c_char_p]),
+    "sm_svd_driver": (C.c_int, []),
+    "sm_simplify_guess": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, dp, ip, C.POINTER(vp), dp, dp,
+                                    ip, C.POINTER(vp), stp, C.c_int, C.POINTER(vp), i64p, ip,
+                                    C.POINTER(sm_simplify_report), vp]),
     "sm_simplify": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, dp, ip, C.POINTER(vp), dp, stp,
                               C.c_int, C.POINTER(vp), i64p, ip, C.POINTER(sm_simplify_report), vp]),
     "sm_simplify_gram": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, dp, ip, C.POINTER(vp), dp,

@@ -325,6 +325,166 @@ def _join_environments(rhoL, rhoR):
     return (rhoL.reshape(-1) * rhoR.transpose(0, 1).reshape(-1)).sum().item()
 
 
+def _canonical_buffers(state: list, cplx: bool):
+    """Private device copies of a list of site tensors, flat, with their bonds."""
+    bufs = [as_device(t, cplx).clone().reshape(-1) for t in state]
+    phys = [int(t.shape[1]) for t in state]
+    bonds = [int(state[0].shape[0])] + [int(t.shape[2]) for t in state]
+    return bufs, phys, bonds
+
+
+def _write_back(state: list, bufs, phys, bonds):
+    for i in range(len(state)):
+        n = bonds[i] * phys[i] * bonds[i + 1]
+        state[i] = bufs[i][:n].view(bonds[i], phys[i], bonds[i + 1])
+
+
+def _canonicalize(state: list, center: int, truncation: Strategy) -> float:
+    """Bring a list of site tensors to canonical form about `center`, in place
+    (cython/schmidt.pxi:109-120): right updates below the centre, left updates above it,
+    each a truncated SVD.  The list's entries are replaced by device tensors; returns the
+    summed sqrt(discarded weight)."""
+    if not isinstance(state, list):
+        raise TypeError("_canonicalize needs a list of tensors")
+    L = len(state)
+    if not 0 <= center < L:
+        raise IndexError("center out of range")
+    bufs, phys, bonds = _canonical_buffers(state, _common_complex(state))
+    cb = _lib.int_array(bonds)
+    err = C.c_double()
+    _lib.check(_lib.load().sm_canonicalize(
+        _lib.context(), dtype_code(bufs[0]), L, _lib.int_array(phys), cb, _lib.ptr_array(bufs),
+        _lib.i64_array([b.numel() for b in bufs]), center, C.byref(truncation.to_c()),
+        C.byref(err), _lib.stream_handle()))
+    _write_back(state, bufs, phys, list(cb))
+    return err.value
+
+
+def _recanonicalize(state: list, oldcenter: int, newcenter: int, truncation: Strategy) -> float:
+    """Move the orthogonality centre of a canonical list of site tensors from `oldcenter`
+    to `newcenter` one site at a time, in place (cython/schmidt.pxi:96-106)."""
+    if not isinstance(state, list):
+        raise TypeError("_recanonicalize needs a list of tensors")
+    L = len(state)
+    if not (0 <= oldcenter < L and 0 <= newcenter < L):
+        raise IndexError("center out of range")
+    bufs, phys, bonds = _canonical_buffers(state, _common_complex(state))
+    cb = _lib.int_array(bonds)
+    err = C.c_double()
+    _lib.check(_lib.load().sm_recanonicalize(
+        _lib.context(), dtype_code(bufs[0]), L, _lib.int_array(phys), cb, _lib.ptr_array(bufs),
+        _lib.i64_array([b.numel() for b in bufs]), oldcenter, newcenter,
+        C.byref(truncation.to_c()), C.byref(err), _lib.stream_handle()))
+    _write_back(state, bufs, phys, list(cb))
+    return err.value
+
+
+def _update_in_canonical_form_right(state: list, A, site: int, truncation: Strategy):
+    """Insert A at `site` and move the centre one site right (cython/schmidt.pxi:18-56):
+    A = U s V truncated, state[site] = U, state[site+1] = (s V) state[site+1].  Returns
+    (new centre, sqrt(discarded weight)); at the last site A is stored as is."""
+    torch = _torch()
+    if site + 1 == len(state):
+        state[site] = A
+        return site, 0.0
+    cplx = _common_complex([A, state[site + 1]])
+    A = as_device(A, cplx)
+    nxt = as_device(state[site + 1], cplx)
+    a, i, b = A.shape
+    b2, j, c = nxt.shape
+    if b2 != b:
+        raise ValueError("Invalid arguments to _update_in_canonical_form_right")
+    r = min(a * i, b)
+    U = torch.empty(a * i * r, dtype=A.dtype, device=A.device)
+    out = torch.empty(r * j * c, dtype=A.dtype, device=A.device)
+    D = C.c_int()
+    err = C.c_double()
+    _lib.check(_lib.load().sm_update_in_canonical_form_right(
+        _lib.context(), dtype_code(A), _lib.ptr(A), a, i, b, _lib.ptr(nxt), j, c,
+        C.byref(truncation.to_c()), _lib.ptr(U), _lib.ptr(out), C.byref(D), C.byref(err),
+        _lib.stream_handle()))
+    D = D.value
+    state[site] = U[: a * i * D].view(a, i, D)
+    state[site + 1] = out[: D * j * c].view(D, j, c)
+    return site + 1, err.value
+
+
+def _update_in_canonical_form_left(state: list, A, site: int, truncation: Strategy):
+    """Insert A at `site` and move the centre one site left (cython/schmidt.pxi:59-93):
+    A = U s V truncated, state[site] = V, state[site-1] = state[site-1] (U s).  Returns
+    (new centre, sqrt(discarded weight)); at site 0 A is stored as is."""
+    torch = _torch()
+    if site == 0:
+        state[0] = A
+        return 0, 0.0
+    cplx = _common_complex([A, state[site - 1]])
+    A = as_device(A, cplx)
+    prv = as_device(state[site - 1], cplx)
+    a, i, b = A.shape
+    p, j, a2 = prv.shape
+    if a2 != a:
+        raise ValueError("Invalid arguments to _update_in_canonical_form_left")
+    r = min(a, i * b)
+    V = torch.empty(r * i * b, dtype=A.dtype, device=A.device)
+    out = torch.empty(p * j * r, dtype=A.dtype, device=A.device)
+    D = C.c_int()
+    err = C.c_double()
+    _lib.check(_lib.load().sm_update_in_canonical_form_left(
+        _lib.context(), dtype_code(A), _lib.ptr(A), a, i, b, _lib.ptr(prv), p, j,
+        C.byref(truncation.to_c()), _lib.ptr(V), _lib.ptr(out), C.byref(D), C.byref(err),
+        _lib.stream_handle()))
+    D = D.value
+    state[site] = V[: D * i * b].view(D, i, b)
+    state[site - 1] = out[: p * j * D].view(p, j, D)
+    return site - 1, err.value
+
+
+def _contract_nrjl_ijk_klm(U, A, B):
+    """np.einsum('ijk,klm,nrjl -> inrm', A, B, U) with U (n*r x j*l)
+    (cython/contractions.pxi:102-127); the result has A's and B's physical shapes."""
+    torch = _torch()
+    cplx = _common_complex([U, A, B])
+    U, A, B = as_device(U, cplx), as_device(A, cplx), as_device(B, cplx)
+    if A.ndim != 3 or B.ndim != 3 or U.ndim != 2:
+        raise ValueError("Invalid arguments to _contract_nrjl_ijk_klm")
+    a, d, b = A.shape
+    b2, e, c = B.shape
+    if b2 != b or U.shape != (d * e, d * e):
+        raise ValueError("Invalid arguments to _contract_nrjl_ijk_klm")
+    out = torch.empty((a, d, e, c), dtype=A.dtype, device=A.device)
+    _lib.check(_lib.load().sm_contract_nrjl_ijk_klm(
+        _lib.context(), dtype_code(A), _lib.ptr(U), d * e, _lib.ptr(A), a, d, b, _lib.ptr(B), e, c,
+        _lib.ptr(out), _lib.stream_handle()))
+    return out
+
+
+def _select_svd_driver(name: str) -> None:
+    """Select the reference's LAPACK SVD driver by name (cython/svd.pxi:25-32): "gesdd" or
+    "gesvd", else ValueError.  The device SVD is one algorithm whose kept ranks and singular
+    values agree with either driver's, so the choice is recorded and changes no result."""
+    if _lib.load().sm_select_svd_driver(str(name).encode()) != _lib.SM_OK:
+        raise ValueError(f"Invalid LAPACK SVD driver name: {name}")
+
+
+def _tensor2site(L, A, B, R):
+    """LA = L A, BR = B R, AA = LA BR: the two-site tensor [l, d1, d2, r] of an
+    AntilinearForm (state/antilinear.py:68-98), one library call."""
+    torch = _torch()
+    cplx = _common_complex([L, A, B, R])
+    L, A, B, R = (as_device(x, cplx) for x in (L, A, B, R))
+    l, i = L.shape
+    i2, d1, k = A.shape
+    k2, d2, n = B.shape
+    n2, r = R.shape
+    if i2 != i or k2 != k or n2 != n:
+        raise ValueError("Invalid arguments to tensor2site")
+    out = torch.empty((l, d1, d2, r), dtype=A.dtype, device=A.device)
+    _lib.check(_lib.load().sm_tensor2site(
+        _lib.context(), dtype_code(A), _lib.ptr(L), l, i, _lib.ptr(A), d1, k, _lib.ptr(B), d2, n,
+        _lib.ptr(R), r, _lib.ptr(out), _lib.stream_handle()))
+    return out
+
+
 def _mpo_multiply_tensor(O, B):
     """C[c*a, i, d*b] = sum_j B[c,j,d] O[a,i,j,b] (operators/mpo.py:26-45)."""
     torch = _torch()

@@ -13,7 +13,8 @@ namespace sm {
 template <typename T>
 int simplify_impl(Ctx&, cudaStream_t, int, const int*, int, const double*, const double*,
                   const int*, const void* const*, const sm_strategy&, int, void* const*,
-                  const int64_t*, int*, sm_simplify_report*, const double*);
+                  const int64_t*, int*, sm_simplify_report*, const double*, const int*,
+                  const void* const*);
 template <typename T>
 int mpo_scprod_impl(Ctx&, cudaStream_t, int, const int*, const int*, const int*,
                     const void* const*, const int*, const void* const*, const int*,
@@ -24,6 +25,9 @@ int canonicalize_impl(Ctx&, cudaStream_t, int, const int*, int*, void* const*, c
 template <typename T>
 int scprod_impl(Ctx&, cudaStream_t, int, const int*, const int*, const void* const*, const int*,
                 const void* const*, double*);
+template <typename T>
+int recanonicalize_impl(Ctx&, cudaStream_t, int, const int*, int*, void* const*, const int64_t*,
+                        int, int, const sm_strategy&, double*);
 
 static thread_local std::string g_error;
 static std::atomic<long long> g_launches{0};
@@ -174,6 +178,105 @@ static int env_right(Ctx* ctx, cudaStream_t st, const void* B, int l, int j, int
   return gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_C, i, l, j * n, one, tmp, j * n, (const T*)B, j * n,
                      zero, (T*)out, l);
 }
+
+// out[j][i][k] = in[i][j][k] for an n0 x n1 x n2 array (swap of the first two axes).
+template <typename T>
+__global__ void k_swap01(const T* __restrict__ in, int n0, int n1, int n2, T* __restrict__ out) {
+  const size_t total = (size_t)n0 * n1 * n2;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < total;
+       x += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = x % n2;
+    const size_t r = x / n2;
+    const size_t j = r % n1;
+    const size_t i = r / n1;
+    out[(j * n0 + i) * n2 + k] = in[x];
+  }
+}
+
+template <typename T>
+static int swap01(cudaStream_t st, const T* in, int n0, int n1, int n2, T* out) {
+  const size_t total = (size_t)n0 * n1 * n2;
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>((total + 255) / 256, 152 * 16));
+  k_swap01<T><<<blocks, 256, 0, st>>>(in, n0, n1, n2, out);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
+}
+
+// _update_in_canonical_form_right (cython/schmidt.pxi:18-42): split A (a*i x b),
+// U -> U_out (a, i, D), (s V) @ next -> next_out (D, j, c).
+template <typename T>
+static int canon_update_right(Ctx* ctx, cudaStream_t st, const T* A, int a, int i, int b,
+                              const T* next, int j, int c, const sm_strategy& s, T* U,
+                              T* next_out, int* D, double* err) {
+  const int r = std::min(a * i, b);
+  T* sv;
+  SM_CHECK(ctx->scratch("kt.sv", (size_t)r * b, &sv));
+  SplitResult res;
+  SM_CHECK(svd_split<T>(*ctx, st, A, a * i, b, s, OUT_U, U, OUT_SVT, sv, nullptr, &res));
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, res.D, j * c, b, S<T>::one(), sv, b, next,
+                       j * c, S<T>::zero(), next_out, j * c));
+  *D = res.D;
+  *err = std::sqrt(res.err2);
+  return SM_OK;
+}
+
+// _update_in_canonical_form_left (cython/schmidt.pxi:59-82): split A (a x i*b),
+// V -> V_out (D, i, b), prev @ (U s) -> prev_out (p, j, D).
+template <typename T>
+static int canon_update_left(Ctx* ctx, cudaStream_t st, const T* A, int a, int i, int b,
+                             const T* prev, int p, int j, const sm_strategy& s, T* V,
+                             T* prev_out, int* D, double* err) {
+  const int r = std::min(a, i * b);
+  T* us;
+  SM_CHECK(ctx->scratch("kt.us", (size_t)a * r, &us));
+  SplitResult res;
+  SM_CHECK(svd_split<T>(*ctx, st, A, a, i * b, s, OUT_US, us, OUT_VT, V, nullptr, &res));
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, p * j, res.D, a, S<T>::one(), prev, a, us,
+                       res.D, S<T>::zero(), prev_out, res.D));
+  *D = res.D;
+  *err = std::sqrt(res.err2);
+  return SM_OK;
+}
+
+// _contract_nrjl_ijk_klm (cython/contractions.pxi:102-127):
+// out[i, x, m] = sum_y U[x, y] (A B)[i, y, m], with (A B)[i, (j l), m] =
+// sum_k A[i, j, k] B[k, l, m].  Formed as one product A B, a swap of its first
+// two axes, one product with U and the swap back.
+template <typename T>
+static int contract_nrjl(Ctx* ctx, cudaStream_t st, const T* U, int nr, const T* A, int a, int d,
+                         int b, const T* B, int e, int c, T* out) {
+  const int de = d * e;
+  const size_t n = (size_t)a * de * c;
+  T *ab, *sw;
+  SM_CHECK(ctx->scratch("kt.ab", n, &ab));
+  SM_CHECK(ctx->scratch("kt.sw", n, &sw));
+  const T one = S<T>::one(), zero = S<T>::zero();
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, a * d, e * c, b, one, A, b, B, e * c, zero, ab,
+                       e * c));
+  SM_CHECK(swap01<T>(st, ab, a, de, c, sw));                     // (de, a, c)
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, nr, a * c, de, one, U, de, sw, a * c, zero, ab,
+                       a * c));                                    // (nr, a, c)
+  return swap01<T>(st, ab, nr, a, c, out);                         // (a, nr, c)
+}
+
+// AntilinearForm.tensor2site (state/antilinear.py:68-98): out[l, d1, d2, r] =
+// sum L[l, i] A[i, d1, k] B[k, d2, n] R[n, r].
+template <typename T>
+static int tensor2site(Ctx* ctx, cudaStream_t st, const T* L, int l, int i, const T* A, int d1,
+                       int k, const T* B, int d2, int n, const T* R, int r, T* out) {
+  T *la, *br;
+  SM_CHECK(ctx->scratch("kt.la", (size_t)l * d1 * k, &la));
+  SM_CHECK(ctx->scratch("kt.br", (size_t)k * d2 * r, &br));
+  const T one = S<T>::one(), zero = S<T>::zero();
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, l, d1 * k, i, one, L, i, A, d1 * k, zero, la,
+                       d1 * k));
+  SM_CHECK(gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, k * d2, r, n, one, B, n, R, r, zero, br, r));
+  return gemm_ctx<T>(*ctx, st, SM_OP_N, SM_OP_N, l * d1, d2 * r, k, one, la, k, br, d2 * r, zero,
+                     out, d2 * r);
+}
+
+static std::atomic<int> g_svd_driver{0};  // 0 = gesdd, 1 = gesvd (the reference's default: gesdd)
 
 }  // namespace sm
 
@@ -531,6 +634,60 @@ int sm_mpo_multiply_tensor(void* ctx, int dtype, const void* O, int a, int i, in
                                    d, (cplx*)C);
 }
 
+static int check_mpo_env(int a, int j, int d, int c, int i, int e, int b, int f,
+                         const void* rho, const void* A, const void* O, const void* B,
+                         const void* out) {
+  if (a <= 0 || j <= 0 || d <= 0 || c <= 0 || i <= 0 || e <= 0 || b <= 0 || f <= 0 || !rho || !A ||
+      !O || !B || !out) {
+    set_error("Invalid arguments to an MPO environment update");
+    return SM_ERR_VALUE;
+  }
+  return SM_OK;
+}
+
+int sm_update_left_mpo_environment(void* ctx, int dtype, const void* rho, const void* A, int a,
+                                   int j, int d, const void* O, int c, int i, int e, const void* B,
+                                   int b, int f, void* out, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_mpo_env(a, j, d, c, i, e, b, f, rho, A, O, B, out));
+  if (dtype == SM_FLOAT64)
+    return mpo_env_left<double>(*as_ctx(ctx), as_stream(stream), (const double*)rho,
+                                (const double*)A, a, j, d, (const double*)O, c, i, e,
+                                (const double*)B, b, f, (double*)out);
+  return mpo_env_left<cplx>(*as_ctx(ctx), as_stream(stream), (const cplx*)rho, (const cplx*)A, a,
+                            j, d, (const cplx*)O, c, i, e, (const cplx*)B, b, f, (cplx*)out);
+}
+
+int sm_update_right_mpo_environment(void* ctx, int dtype, const void* rho, const void* A, int a,
+                                    int j, int d, const void* O, int c, int i, int e,
+                                    const void* B, int b, int f, void* out, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_mpo_env(a, j, d, c, i, e, b, f, rho, A, O, B, out));
+  if (dtype == SM_FLOAT64)
+    return mpo_env_right<double>(*as_ctx(ctx), as_stream(stream), (const double*)rho,
+                                 (const double*)A, a, j, d, (const double*)O, c, i, e,
+                                 (const double*)B, b, f, (double*)out);
+  return mpo_env_right<cplx>(*as_ctx(ctx), as_stream(stream), (const cplx*)rho, (const cplx*)A, a,
+                             j, d, (const cplx*)O, c, i, e, (const cplx*)B, b, f, (cplx*)out);
+}
+
+int sm_mpo_join(void* ctx, int dtype, const void* B, int a, int i, int j, int b, const void* A,
+                int c, int k, int d, void* C, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (a <= 0 || i <= 0 || j <= 0 || b <= 0 || c <= 0 || k <= 0 || d <= 0 || !A || !B || !C) {
+    set_error("Invalid arguments to MPOList.join");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return mpo_join<double>(as_stream(stream), (const double*)B, a, i, j, b, (const double*)A, c, k,
+                            d, (double*)C);
+  return mpo_join<cplx>(as_stream(stream), (const cplx*)B, a, i, j, b, (const cplx*)A, c, k, d,
+                        (cplx*)C);
+}
+
 int sm_scprod(void* ctx, int dtype, int L, const int* phys, const int* bra_bonds,
               const void* const* bra, const int* ket_bonds, const void* const* ket, double* out,
               void* stream) {
@@ -564,11 +721,116 @@ int sm_canonicalize(void* ctx, int dtype, int L, const int* phys, int* bonds, vo
                                  center, *st, err);
 }
 
+int sm_recanonicalize(void* ctx, int dtype, int L, const int* phys, int* bonds, void* const* sites,
+                      const int64_t* cap, int oldcenter, int newcenter, const sm_strategy* st,
+                      double* err, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_strategy(st));
+  if (L < 1 || oldcenter < 0 || oldcenter >= L || newcenter < 0 || newcenter >= L || !err) {
+    set_error("recanonicalize: center out of range");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return recanonicalize_impl<double>(*as_ctx(ctx), as_stream(stream), L, phys, bonds, sites, cap,
+                                       oldcenter, newcenter, *st, err);
+  return recanonicalize_impl<cplx>(*as_ctx(ctx), as_stream(stream), L, phys, bonds, sites, cap,
+                                   oldcenter, newcenter, *st, err);
+}
+
+int sm_update_in_canonical_form_right(void* ctx, int dtype, const void* A, int a, int i, int b,
+                                      const void* next, int j, int c, const sm_strategy* st,
+                                      void* U, void* next_out, int* D, double* err,
+                                      void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_strategy(st));
+  if (a <= 0 || i <= 0 || b <= 0 || j <= 0 || c <= 0 || !A || !next || !U || !next_out || !D ||
+      !err) {
+    set_error("Invalid arguments to _update_in_canonical_form_right");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return canon_update_right<double>(as_ctx(ctx), as_stream(stream), (const double*)A, a, i, b,
+                                      (const double*)next, j, c, *st, (double*)U,
+                                      (double*)next_out, D, err);
+  return canon_update_right<cplx>(as_ctx(ctx), as_stream(stream), (const cplx*)A, a, i, b,
+                                  (const cplx*)next, j, c, *st, (cplx*)U, (cplx*)next_out, D, err);
+}
+
+int sm_update_in_canonical_form_left(void* ctx, int dtype, const void* A, int a, int i, int b,
+                                     const void* prev, int p, int j, const sm_strategy* st, void* V,
+                                     void* prev_out, int* D, double* err, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  SM_CHECK(check_strategy(st));
+  if (a <= 0 || i <= 0 || b <= 0 || p <= 0 || j <= 0 || !A || !prev || !V || !prev_out || !D ||
+      !err) {
+    set_error("Invalid arguments to _update_in_canonical_form_left");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return canon_update_left<double>(as_ctx(ctx), as_stream(stream), (const double*)A, a, i, b,
+                                     (const double*)prev, p, j, *st, (double*)V,
+                                     (double*)prev_out, D, err);
+  return canon_update_left<cplx>(as_ctx(ctx), as_stream(stream), (const cplx*)A, a, i, b,
+                                 (const cplx*)prev, p, j, *st, (cplx*)V, (cplx*)prev_out, D, err);
+}
+
+int sm_contract_nrjl_ijk_klm(void* ctx, int dtype, const void* U, int nr, const void* A, int a,
+                             int d, int b, const void* B, int e, int c, void* out, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (a <= 0 || d <= 0 || b <= 0 || e <= 0 || c <= 0 || nr != d * e || !U || !A || !B || !out) {
+    set_error("Invalid arguments to _contract_nrjl_ijk_klm");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return contract_nrjl<double>(as_ctx(ctx), as_stream(stream), (const double*)U, nr,
+                                 (const double*)A, a, d, b, (const double*)B, e, c, (double*)out);
+  return contract_nrjl<cplx>(as_ctx(ctx), as_stream(stream), (const cplx*)U, nr, (const cplx*)A, a,
+                             d, b, (const cplx*)B, e, c, (cplx*)out);
+}
+
+int sm_tensor2site(void* ctx, int dtype, const void* L, int l, int i, const void* A, int d1, int k,
+                   const void* B, int d2, int n, const void* R, int r, void* out, void* stream) {
+  SM_GUARD_CTX(ctx);
+  SM_CHECK(check_dtype(dtype));
+  if (l <= 0 || i <= 0 || d1 <= 0 || k <= 0 || d2 <= 0 || n <= 0 || r <= 0 || !L || !A || !B ||
+      !R || !out) {
+    set_error("Invalid arguments to tensor2site");
+    return SM_ERR_VALUE;
+  }
+  if (dtype == SM_FLOAT64)
+    return tensor2site<double>(as_ctx(ctx), as_stream(stream), (const double*)L, l, i,
+                               (const double*)A, d1, k, (const double*)B, d2, n, (const double*)R, r,
+                               (double*)out);
+  return tensor2site<cplx>(as_ctx(ctx), as_stream(stream), (const cplx*)L, l, i, (const cplx*)A, d1,
+                           k, (const cplx*)B, d2, n, (const cplx*)R, r, (cplx*)out);
+}
+
+int sm_select_svd_driver(const char* name) {
+  const std::string s = name ? name : "";
+  if (s == "gesdd") {
+    g_svd_driver = 0;
+    return SM_OK;
+  }
+  if (s == "gesvd") {
+    g_svd_driver = 1;
+    return SM_OK;
+  }
+  set_error("Invalid LAPACK SVD driver name: " + s);
+  return SM_ERR_VALUE;
+}
+
+int sm_svd_driver(void) { return g_svd_driver.load(); }
+
 static int simplify_entry(void* ctx, int dtype, int L, const int* phys, int nterms,
                           const double* weights, const int* ket_bonds, const void* const* ket_sites,
                           const double* term_errors, const sm_strategy* st, int direction,
                           void* const* out_sites, const int64_t* out_cap, int* out_bonds,
-                          sm_simplify_report* rep, const double* gram, void* stream) {
+                          sm_simplify_report* rep, const double* gram, const int* guess_bonds,
+                          const void* const* guess_sites, void* stream) {
   SM_GUARD_CTX(ctx);
   SM_CHECK(check_dtype(dtype));
   SM_CHECK(check_strategy(st));
@@ -591,10 +853,10 @@ static int simplify_entry(void* ctx, int dtype, int L, const int* phys, int nter
   if (dtype == SM_FLOAT64)
     return simplify_impl<double>(*as_ctx(ctx), as_stream(stream), L, phys, nterms, weights,
                                  term_errors, ket_bonds, ket_sites, *st, direction, out_sites,
-                                 out_cap, out_bonds, rep, gram);
+                                 out_cap, out_bonds, rep, gram, guess_bonds, guess_sites);
   return simplify_impl<cplx>(*as_ctx(ctx), as_stream(stream), L, phys, nterms, weights,
                              term_errors, ket_bonds, ket_sites, *st, direction, out_sites, out_cap,
-                             out_bonds, rep, gram);
+                             out_bonds, rep, gram, guess_bonds, guess_sites);
 }
 
 int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms, const double* weights,
@@ -602,7 +864,23 @@ int sm_simplify(void* ctx, int dtype, int L, const int* phys, int nterms, const 
                 const sm_strategy* st, int direction, void* const* out_sites,
                 const int64_t* out_cap, int* out_bonds, sm_simplify_report* rep, void* stream) {
   return simplify_entry(ctx, dtype, L, phys, nterms, weights, ket_bonds, ket_sites, term_errors, st,
-                        direction, out_sites, out_cap, out_bonds, rep, nullptr, stream);
+                        direction, out_sites, out_cap, out_bonds, rep, nullptr, nullptr, nullptr,
+                        stream);
+}
+
+int sm_simplify_guess(void* ctx, int dtype, int L, const int* phys, int nterms,
+                      const double* weights, const int* ket_bonds, const void* const* ket_sites,
+                      const double* term_errors, const double* gram, const int* guess_bonds,
+                      const void* const* guess_sites, const sm_strategy* st, int direction,
+                      void* const* out_sites, const int64_t* out_cap, int* out_bonds,
+                      sm_simplify_report* rep, void* stream) {
+  if (!guess_bonds || !guess_sites) {
+    set_error("simplify_guess: the guess must not be null");
+    return SM_ERR_VALUE;
+  }
+  return simplify_entry(ctx, dtype, L, phys, nterms, weights, ket_bonds, ket_sites, term_errors, st,
+                        direction, out_sites, out_cap, out_bonds, rep, gram, guess_bonds,
+                        guess_sites, stream);
 }
 
 int sm_simplify_gram(void* ctx, int dtype, int L, const int* phys, int nterms,
@@ -615,7 +893,8 @@ int sm_simplify_gram(void* ctx, int dtype, int L, const int* phys, int nterms,
     return SM_ERR_VALUE;
   }
   return simplify_entry(ctx, dtype, L, phys, nterms, weights, ket_bonds, ket_sites, term_errors, st,
-                        direction, out_sites, out_cap, out_bonds, rep, gram, stream);
+                        direction, out_sites, out_cap, out_bonds, rep, gram, nullptr, nullptr,
+                        stream);
 }
 
 int sm_mpo_scprod(void* ctx, int dtype, int L, const int* dout, const int* din,

@@ -191,6 +191,15 @@ int two_site_prepare(Ctx& ctx, cudaStream_t st, int a, int c, int b, int p1, int
 int two_site_matvec_prepared(Ctx& ctx, cudaStream_t st, const double* H, const double* v,
                              double* out);
 
+// --- mpo_env.cu --------------------------------------------------------------
+// Three-leg MPO environments (bra A (a, j, d), MPO O (c, j, i, e), ket B (b, i, f)):
+// left rho (a, c, b) -> out (d, e, f); right rho (d, e, f) -> out (a, c, b).
+template <typename T>
+int mpo_env_left(Ctx& ctx, cudaStream_t st, const T* rho, const T* A, int a, int j, int d,
+                 const T* O, int c, int i, int e, const T* B, int b, int f, T* out);
+template <typename T>
+int mpo_env_right(Ctx& ctx, cudaStream_t st, const T* rho, const T* A, int a, int j, int d,
+                  const T* O, int c, int i, int e, const T* B, int b, int f, T* out);
 // --- mps_ops.cu ------------------------------------------------------------
 template <typename T>
 int scale_matrix(cudaStream_t st, int M, int N, T beta, T* C, int ldc);
@@ -201,6 +210,10 @@ int fill_zero(cudaStream_t st, size_t n, T* x);
 template <typename T>
 int mpo_multiply_tensor(cudaStream_t st, const T* O, int a, int i, int j, int b, const T* B,
                         int c, int d, T* C);
+// C[(a c), i, k, (b d)] = sum_j B[a, i, j, b] A[c, j, k, d] (A applied first, then B)
+template <typename T>
+int mpo_join(cudaStream_t st, const T* B, int a, int i, int j, int b, const T* A, int c, int k,
+             int d, T* C);
 // out[0] (+ out[1] for complex) = sum conj(x) y, deterministic two-pass reduction
 template <typename T>
 int vdot(Ctx& ctx, cudaStream_t st, size_t n, const T* x, const T* y, double* out_dev);

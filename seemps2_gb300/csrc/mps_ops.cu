@@ -48,6 +48,29 @@ __global__ void k_mpo_multiply(const T* __restrict__ O, int a_, int i_, int j_, 
   }
 }
 
+// Joined tensor of two MPOs applied one after the other (A first, then B):
+// C[(a c), i, k, (b d)] = sum_j B[a, i, j, b] A[c, j, k, d]; one thread per output.
+template <typename T>
+__global__ void k_mpo_join(const T* __restrict__ B, int a_, int i_, int j_, int b_,
+                           const T* __restrict__ A, int c_, int k_, int d_, T* __restrict__ C) {
+  const size_t total = (size_t)a_ * c_ * i_ * k_ * b_ * d_;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    size_t r = e;
+    const int d = (int)(r % d_); r /= d_;
+    const int b = (int)(r % b_); r /= b_;
+    const int k = (int)(r % k_); r /= k_;
+    const int i = (int)(r % i_); r /= i_;
+    const int c = (int)(r % c_); r /= c_;
+    const int a = (int)r;
+    T acc = S<T>::zero();
+    for (int j = 0; j < j_; ++j)
+      acc = S<T>::fma(B[(((size_t)a * i_ + i) * j_ + j) * b_ + b],
+                      A[(((size_t)c * j_ + j) * k_ + k) * d_ + d], acc);
+    C[e] = acc;
+  }
+}
+
 // B[j, i] = A[i, j], 32x32 tiles through shared memory
 template <typename T>
 __global__ void k_transpose(int m, int n, const T* __restrict__ A, int lda, T* __restrict__ B,
@@ -184,6 +207,17 @@ int mpo_multiply_tensor(cudaStream_t st, const T* O, int a, int i, int j, int b,
 }
 
 template <typename T>
+int mpo_join(cudaStream_t st, const T* B, int a, int i, int j, int b, const T* A, int c, int k,
+             int d, T* C) {
+  const size_t n = (size_t)a * c * i * k * b * d;
+  if (!n) return SM_OK;
+  k_mpo_join<T><<<grid_for<T>(n), 256, 0, st>>>(B, a, i, j, b, A, c, k, d, C);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
+}
+
+template <typename T>
 int vdot(Ctx& ctx, cudaStream_t st, size_t n, const T* x, const T* y, double* out_dev) {
   double* part;
   SM_CHECK(ctx.scratch("vdot.part", 2 * kVdotBlocks, &part));
@@ -234,6 +268,8 @@ int copy_block3(cudaStream_t st, const T* src, int a, int d, int b, T* dst, int 
   template int fill_zero<T>(cudaStream_t, size_t, T*);                                      \
   template int mpo_multiply_tensor<T>(cudaStream_t, const T*, int, int, int, int, const T*, \
                                       int, int, T*);                                        \
+  template int mpo_join<T>(cudaStream_t, const T*, int, int, int, int, const T*, int, int,  \
+                           int, T*);                                                        \
   template int vdot<T>(Ctx&, cudaStream_t, size_t, const T*, const T*, double*);            \
   template int transpose<T>(cudaStream_t, int, int, const T*, int, T*, int);                \
   template int set_identity<T>(cudaStream_t, int, T*, int);                                 \

@@ -293,7 +293,8 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
                   const double* weights, const double* term_errors, const int* ket_bonds,
                   const void* const* ket_sites, const sm_strategy& s, int direction,
                   void* const* out_sites, const int64_t* out_cap, int* out_bonds,
-                  sm_simplify_report* rep, const double* gram) {
+                  sm_simplify_report* rep, const double* gram, const int* guess_bonds,
+                  const void* const* guess_sites) {
   Sweeper<T> S_(ctx, st, s);
   auto& w = S_;
   w.L = L;
@@ -373,7 +374,8 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
   const bool variational = s.simplify != SM_CANONICAL_FORM && s.simplify != SM_DO_NOT_SIMPLIFY;
   if (w.nt == 0) return emit_zero();  // every term of the sum is zero
 
-  // ---- the guess: the joined kets (state/mpssum.py:130-167) ---------------
+  // ---- the guess: the joined kets (state/mpssum.py:130-167), or the caller's
+  // guess (simplification.py:93-98: CanonicalMPS(guess, center=start)) -------
   std::vector<int> K(L + 1, 0);
   K[0] = K[L] = 1;
   for (int i = 1; i < L; ++i) {
@@ -381,12 +383,32 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
     for (int t = 0; t < w.nt; ++t) acc += w.kb[t][i];
     K[i] = acc;
   }
+  const bool has_guess = guess_bonds != nullptr && guess_sites != nullptr && variational;
+  // buffer sizes: the guess's bonds may exceed the joined kets' bonds
+  std::vector<int> KX = K;
+  if (has_guess) {
+    if (guess_bonds[0] != 1 || guess_bonds[L] != 1) {
+      set_error("simplify: the guess's open boundary bonds must be 1");
+      return SM_ERR_VALUE;
+    }
+    for (int i = 0; i <= L; ++i) {
+      if (guess_bonds[i] <= 0) {
+        set_error("simplify: non-positive bond in the guess");
+        return SM_ERR_VALUE;
+      }
+      KX[i] = std::max(K[i], guess_bonds[i]);
+    }
+  }
   const bool unit_single = w.nt == 1 && S<T>::abs2(w.w[0] - S<T>::one()) == 0.0;
-  w.bb = K;
+  w.bb = has_guess ? std::vector<int>(guess_bonds, guess_bonds + L + 1) : K;
   w.bra.resize(L);
   for (int i = 0; i < L; ++i) {
-    SM_CHECK(w.buf("sw.bra." + std::to_string(i), (size_t)K[i] * w.d[i] * K[i + 1], &w.bra[i]));
-    if (unit_single) {
+    SM_CHECK(w.buf("sw.bra." + std::to_string(i), (size_t)KX[i] * w.d[i] * KX[i + 1], &w.bra[i]));
+    if (has_guess) {
+      SM_CUDA_CHECK(cudaMemcpyAsync(w.bra[i], guess_sites[i],
+                                    sizeof(T) * (size_t)guess_bonds[i] * w.d[i] * guess_bonds[i + 1],
+                                    cudaMemcpyDeviceToDevice, st));
+    } else if (unit_single) {
       SM_CUDA_CHECK(cudaMemcpyAsync(w.bra[i], w.ket[0][i], sizeof(T) * (size_t)K[i] * w.d[i] * K[i + 1],
                                     cudaMemcpyDeviceToDevice, st));
     } else {
@@ -408,16 +430,18 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
     }
   }
   // bond caps for the sweep buffers: every split keeps at most min(max bond, K)
+  // (and the guess's own bonds, which the canonical form can only reduce)
   w.cap.assign(L + 1, 1);
-  for (int i = 0; i <= L; ++i) w.cap[i] = std::max(1, std::min(K[i], s.max_bond_dimension));
+  for (int i = 0; i <= L; ++i)
+    w.cap[i] = std::max({1, std::min(K[i], s.max_bond_dimension), has_guess ? guess_bonds[i] : 1});
   w.cap[0] = K[0];
   w.cap[L] = K[L];
   // scratch for the sweep
   size_t mx_tmp = 1, mx_AA = 1;
   for (int i = 0; i < L; ++i) {
-    mx_tmp = std::max(mx_tmp, (size_t)K[i] * w.d[i] * K[i + 1]);
-    mx_tmp = std::max(mx_tmp, (size_t)K[i] * K[i]);
-    mx_tmp = std::max(mx_tmp, (size_t)K[i + 1] * K[i + 1]);
+    mx_tmp = std::max(mx_tmp, (size_t)KX[i] * w.d[i] * KX[i + 1]);
+    mx_tmp = std::max(mx_tmp, (size_t)KX[i] * KX[i]);
+    mx_tmp = std::max(mx_tmp, (size_t)KX[i + 1] * KX[i + 1]);
     if (i + 1 < L)
       mx_AA = std::max(mx_AA, (size_t)w.cap[i] * w.d[i] * w.d[i + 1] * w.cap[i + 2]);
   }
@@ -554,6 +578,33 @@ int canonicalize_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int* bo
   return SM_OK;
 }
 
+// In-place move of the orthogonality centre (cython/schmidt.pxi:96-106).
+template <typename T>
+int recanonicalize_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int* bonds,
+                        void* const* sites, const int64_t* cap, int oldc, int newc,
+                        const sm_strategy& s, double* err) {
+  Sweeper<T> w(ctx, st, s);
+  w.L = L;
+  w.d.assign(phys, phys + L);
+  w.bb.assign(bonds, bonds + L + 1);
+  w.bra.resize(L);
+  size_t mx = 1;
+  for (int i = 0; i < L; ++i) {
+    w.bra[i] = reinterpret_cast<T*>(sites[i]);
+    if ((size_t)cap[i] < w.site_elems(i)) {
+      set_error("recanonicalize: site buffer smaller than its tensor");
+      return SM_ERR_VALUE;
+    }
+    mx = std::max(mx, w.site_elems(i));
+  }
+  SM_CHECK(w.buf("cn.tmp", mx, &w.tmp));
+  SM_CHECK(w.buf("cn.tmp2", mx, &w.tmp2));
+  SM_CHECK(w.recanonicalize(oldc, newc, err));
+  for (int i = 0; i <= L; ++i) bonds[i] = w.bb[i];
+  SM_CUDA_CHECK(cudaStreamSynchronize(st));
+  return SM_OK;
+}
+
 template <typename T>
 int scprod_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, const int* ab,
                 const void* const* A, const int* bbnd, const void* const* B, double* out) {
@@ -571,9 +622,12 @@ int scprod_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, const int* ab
   template int simplify_impl<T>(Ctx&, cudaStream_t, int, const int*, int, const double*,       \
                                 const double*, const int*, const void* const*,                 \
                                 const sm_strategy&, int, void* const*, const int64_t*, int*,   \
-                                sm_simplify_report*, const double*);                           \
+                                sm_simplify_report*, const double*, const int*,                \
+                                const void* const*);                                           \
   template int canonicalize_impl<T>(Ctx&, cudaStream_t, int, const int*, int*, void* const*,   \
                                     const int64_t*, int, const sm_strategy&, double*);         \
+  template int recanonicalize_impl<T>(Ctx&, cudaStream_t, int, const int*, int*, void* const*, \
+                                      const int64_t*, int, int, const sm_strategy&, double*);  \
   template int scprod_impl<T>(Ctx&, cudaStream_t, int, const int*, const int*,                 \
                               const void* const*, const int*, const void* const*, double*);
 SM_INST2(double)

@@ -7,8 +7,9 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .core import DEFAULT_STRATEGY, Strategy, _mpo_multiply_tensor, as_device
-from .state import MPS, MPSSum, TensorArray, _simplify_terms, simplify
+from .core import (DEFAULT_STRATEGY, NO_TRUNCATION, Simplification, Strategy,
+                   _mpo_multiply_tensor, as_device, dtype_code)
+from .state import SIMPLIFICATION_STRATEGY, MPS, MPSSum, TensorArray, _simplify_terms, simplify
 
 
 class MPO(TensorArray):
@@ -197,3 +198,77 @@ class MPOList:
         if isinstance(b, MPOList):
             return MPOList(b.mpos + self.mpos, self.strategy)
         raise TypeError(f"Cannot multiply MPOList with {b}")
+
+    def join(self, strategy: Strategy | None = None) -> MPO:
+        """One MPO for the product of the list (operators/mpo.py:679-711): at each site the
+        tensors are joined pairwise from the last MPO backwards, C[(a c), i, k, (b d)] =
+        sum_j B[a, i, j, b] A[c, j, k, d] with A applied before B (sm_mpo_join)."""
+        import torch
+
+        cplx = any(m[0].is_complex() for m in self.mpos)
+
+        def join2(A, B):  # A applied first, then B
+            A = as_device(A, cplx)
+            B = as_device(B, cplx)
+            a, i, j, b = B.shape
+            c, j2, k, d = A.shape
+            if j2 != j:
+                raise ValueError("MPOList.join: physical dimensions differ")
+            out = torch.empty((a * c, i, k, b * d), dtype=A.dtype, device=A.device)
+            _lib.check(_lib.load().sm_mpo_join(_lib.context(), dtype_code(A), _lib.ptr(B), a, i, j,
+                                               b, _lib.ptr(A), c, k, d, _lib.ptr(out),
+                                               _lib.stream_handle()))
+            return out
+
+        tensors = []
+        for s in range(self.size):
+            ts = [m[s] for m in self.mpos]
+            acc = ts[-1]
+            for A in reversed(ts[:-1]):
+                acc = join2(A, acc)
+            tensors.append(acc)
+        return MPO(tensors, self.strategy if strategy is None else strategy)
+
+
+#: MPO simplification does not normalise by default (operators/simplify_mpo.py:18-19)
+MPO_SIMPLIFICATION_STRATEGY = SIMPLIFICATION_STRATEGY.replace(normalize=False)
+#: canonical forms without truncation (operators/simplify_mpo.py:15-16)
+CANONICALIZE_MPO = NO_TRUNCATION.replace(simplify=Simplification.DO_NOT_SIMPLIFY)
+
+
+def mpo_as_mps(mpo: MPO) -> MPS:
+    """The MPO's sites O[a, i, j, b] as MPS sites [a, (i j), b] (operators/simplify_mpo.py:22-29)."""
+    return MPS([A.reshape(A.shape[0], A.shape[1] * A.shape[2], A.shape[3]) for A in mpo._data])
+
+
+def mps_as_mpo(mps: MPS, mpo_strategy: Strategy = DEFAULT_STRATEGY) -> MPO:
+    """MPS sites [a, p, b] with p a perfect square as MPO sites [a, s, s, b]
+    (operators/simplify_mpo.py:32-47)."""
+    from math import isqrt
+
+    data = []
+    for A in mps._data:
+        bl, p, br = A.shape
+        s = isqrt(p)
+        if s * s != p:
+            raise ValueError("The physical dimensions of the MPS must be a perfect square")
+        data.append(A.reshape(bl, s, s, br))
+    return MPO(data, strategy=mpo_strategy)
+
+
+def simplify_mpo(operator, strategy: Strategy = MPO_SIMPLIFICATION_STRATEGY, direction: int = +1,
+                 guess: MPO | None = None, mpo_strategy: Strategy | None = None) -> MPO:
+    """Approximate an MPO (or the product of an MPOList) by one of smaller bond dimension
+    (operators/simplify_mpo.py:50-89): the operator is recast as an MPS of physical
+    dimension i*j, simplified variationally on the device (with the guess, if any, as the
+    starting state) and recast as an MPO."""
+    if isinstance(operator, MPOList):
+        operator = operator.join()
+    if not isinstance(operator, MPO):
+        raise TypeError(f"Cannot simplify {type(operator)} as an MPO")
+    if mpo_strategy is None:
+        mpo_strategy = operator.strategy
+    mps = mpo_as_mps(operator)
+    guess_mps = None if guess is None else mpo_as_mps(guess)
+    out = simplify(mps, strategy, direction, guess_mps)
+    return mps_as_mpo(out, mpo_strategy=mpo_strategy)

@@ -226,6 +226,76 @@ def scprod(bra: MPS, ket: MPS):
 vdot = scprod
 
 
+class AntilinearForm:
+    """<bra|ket> with the environments kept left and right of `center`
+    (state/antilinear.py:13-146): tensor1site / tensor2site give the tensors whose
+    contraction with the bra's site(s) is the form; update_right / update_left move the
+    centre after the bra changed.  Every contraction is a library call."""
+
+    def __init__(self, bra: MPS, ket: MPS, center: int = 0):
+        from .core import _begin_environment, _update_left_environment, _update_right_environment
+
+        if bra.size != ket.size:
+            raise ValueError("bra and ket must have the same size")
+        size = bra.size
+        rho = _begin_environment()
+        R = [rho] * size
+        for i in range(size - 1, center, -1):
+            R[i - 1] = rho = _update_right_environment(bra[i], ket[i], rho)
+        rho = _begin_environment()
+        Lv = [rho] * size
+        for i in range(0, center):
+            Lv[i + 1] = rho = _update_left_environment(bra[i], ket[i], rho)
+        self.bra, self.ket, self.size = bra, ket, size
+        self.R, self.L, self.center = R, Lv, center
+
+    def tensor1site(self):
+        """L[c] ket[c] R[c] (antilinear.py:59-66)."""
+        from .core import _contract_last_and_first
+
+        c = self.center
+        return _contract_last_and_first(self.L[c], _contract_last_and_first(self.ket[c], self.R[c]))
+
+    def tensor2site(self, direction: int):
+        """The two-site tensor on (center, center+1) if direction > 0, else on
+        (center-1, center) (antilinear.py:68-98)."""
+        from .core import _tensor2site
+
+        if direction > 0:
+            i = self.center
+            j = i + 1
+        else:
+            j = self.center
+            i = j - 1
+        return _tensor2site(self.L[i], self.ket[i], self.ket[j], self.R[j])
+
+    def update(self, direction: int) -> None:
+        if direction > 0:
+            self.update_right()
+        else:
+            self.update_left()
+
+    def update_right(self) -> None:
+        from .core import _update_left_environment
+
+        prev = self.center
+        nxt = prev + 1
+        if nxt >= self.size:
+            raise RuntimeError("Cannot move the center beyond the last site")
+        self.L[nxt] = _update_left_environment(self.bra[prev], self.ket[prev], self.L[prev])
+        self.center = nxt
+
+    def update_left(self) -> None:
+        from .core import _update_right_environment
+
+        prev = self.center
+        nxt = prev - 1
+        if nxt < 0:
+            raise RuntimeError("Cannot move the center before the first site")
+        self.R[nxt] = _update_right_environment(self.bra[prev], self.ket[prev], self.R[prev])
+        self.center = nxt
+
+
 class CanonicalMPS(MPS):
     """MPS in canonical form with respect to `center` (state/canonical_mps.py:38-108)."""
 
@@ -447,11 +517,16 @@ last_report: dict = {}
 
 
 def _simplify_terms(weights, states, strategy: Strategy, direction: int,
-                    gram=None) -> CanonicalMPS:
+                    gram=None, guess: MPS | None = None) -> CanonicalMPS:
     """simplify of sum_t w_t |s_t>; `gram` (optional, nterms x nterms complex,
-    <s_i|s_j>) replaces the terms' scprods in the state norm."""
+    <s_i|s_j>) replaces the terms' scprods in the state norm; `guess` (optional) is the
+    sweeps' starting state instead of the joined terms."""
     torch = _torch()
     cplx = any(isinstance(w, complex) and w.imag != 0 for w in weights) or any(s.is_complex() for s in states)
+    if guess is not None:
+        if guess.size != states[0].size or guess.physical_dimensions() != states[0].physical_dimensions():
+            raise ValueError("simplify: the guess does not match the state's sites")
+        cplx = cplx or guess.is_complex()
     states = [s if (s.is_complex() == cplx) else MPS(s._data, s._error) for s in states]
     kets = [[as_device(t, cplx) for t in s._data] for s in states]
     L, phys, bonds, _ = _site_arrays(states)
@@ -462,6 +537,12 @@ def _simplify_terms(weights, states, strategy: Strategy, direction: int,
                                                  _lib.int_array(bonds), C.byref(st_c), caps))
     dt = torch.complex128 if cplx else torch.float64
     dev = kets[0][0].device
+    gsites = gbonds = None
+    if guess is not None:
+        gsites = [as_device(t, cplx) for t in guess._data]
+        gbonds = guess.bond_dimensions()
+        for i in range(L + 1):
+            caps[i] = max(caps[i], gbonds[i])
     outs = [torch.empty(max(1, caps[i] * phys[i] * caps[i + 1]), dtype=dt, device=dev)
             for i in range(L)]
     wpairs = []
@@ -476,12 +557,18 @@ def _simplify_terms(weights, states, strategy: Strategy, direction: int,
             _lib.ptr_array(flat), _lib.dbl_array([s._error for s in states]))
     tail = (C.byref(st_c), int(direction), _lib.ptr_array(outs),
             _lib.i64_array([o.numel() for o in outs]), out_bonds, C.byref(rep), _lib.stream_handle())
-    if gram is None:
-        _lib.check(_lib.load().sm_simplify(*head, *tail))
-    else:
+    gram_arr = None
+    if gram is not None:
         g = np.asarray(gram, dtype=complex).reshape(nterms, nterms)
         pairs = np.stack([g.real, g.imag], axis=-1).reshape(-1)
-        _lib.check(_lib.load().sm_simplify_gram(*head, _lib.dbl_array(pairs.tolist()), *tail))
+        gram_arr = _lib.dbl_array(pairs.tolist())
+    if guess is not None:
+        _lib.check(_lib.load().sm_simplify_guess(*head, gram_arr, _lib.int_array(gbonds),
+                                                 _lib.ptr_array(gsites), *tail))
+    elif gram is None:
+        _lib.check(_lib.load().sm_simplify(*head, *tail))
+    else:
+        _lib.check(_lib.load().sm_simplify_gram(*head, gram_arr, *tail))
     data = [outs[i][: out_bonds[i] * phys[i] * out_bonds[i + 1]].view(out_bonds[i], phys[i],
                                                                          out_bonds[i + 1])
             for i in range(L)]
@@ -500,13 +587,14 @@ def _simplify_terms(weights, states, strategy: Strategy, direction: int,
 
 def simplify(state, strategy: Strategy = SIMPLIFICATION_STRATEGY, direction: int = +1,
              guess: MPS | None = None) -> CanonicalMPS:
-    """Simplify an MPS or MPSSum (state/simplification.py:32-144, :150-280)."""
-    if guess is not None:
-        raise NotImplementedError("simplify(guess=...) is not supported by the GPU path yet")
+    """Simplify an MPS or MPSSum (state/simplification.py:32-144, :150-280); a `guess`
+    starts the variational sweeps instead of the state itself (:93-98, :214-219)."""
+    if guess is not None and not isinstance(guess, MPS):
+        raise TypeError("simplify: the guess must be an MPS")
     if isinstance(state, MPSSum):
-        return _simplify_terms(state.weights, state.states, strategy, direction)
+        return _simplify_terms(state.weights, state.states, strategy, direction, guess=guess)
     if isinstance(state, MPS):
-        return _simplify_terms([1.0], [state], strategy, direction)
+        return _simplify_terms([1.0], [state], strategy, direction, guess=guess)
     raise TypeError(f"Cannot simplify {type(state)}")
 
 

@@ -25,6 +25,8 @@ def load_case(name: str):
     mps, mpo = mg.make_inputs(p)
     same_inputs = mg.input_hash(mps, mpo) == meta["input_sha256"]
     g = {k: z[k] for k in z.files if k != "meta"}
+    if "split_full_len" not in g:
+        g["split_full_len"] = g["split_len"]
     offs = np.concatenate([[0], np.cumsum(g["split_len"])])
     g["splits_s"] = [g["split_s"][offs[i]:offs[i + 1]] for i in range(len(g["split_len"]))]
     return p, mps, mpo, g, same_inputs
@@ -54,4 +56,5 @@ def truncation_cases():
     return [(np.array(d["vectors"][c["v"]]), c) for c in d["cases"]]
 
 
-CASE_NAMES = ["c1_small", "c1", "lap_small", "lap_n30_chi32", "euler_small", "simplify_real"]
+CASE_NAMES = ["c1_small", "c1", "lap_small", "lap_n30_chi32", "euler_small", "simplify_real",
+              "c2", "northstar"]

@@ -89,3 +89,39 @@ def test_no_cpu_fallback_without_gpu():
 
     with pytest.raises(RuntimeError):
         _lib.context()
+
+
+# The reference's kernel table, cython/__init__.py:25-54 (configuration names and kernels).
+REFERENCE_CONFIG = ["DEFAULT_STRATEGY", "DEFAULT_TOLERANCE", "GemmOrder", "MAX_BOND_DIMENSION",
+                    "NO_TRUNCATION", "Simplification", "Strategy", "Truncation"]
+REFERENCE_KERNELS = ["_begin_environment", "_canonicalize", "_contract_last_and_first",
+                     "_contract_nrjl_ijk_klm", "_destructive_svd", "_end_environment", "_gemm",
+                     "_join_environments", "_left_orth_2site", "_right_orth_2site",
+                     "_recanonicalize", "_select_svd_driver", "_update_in_canonical_form_right",
+                     "_update_in_canonical_form_left", "_update_left_environment",
+                     "_update_right_environment", "destructively_truncate_vector", "scprod",
+                     "vdot"]
+
+
+def test_kernel_table_has_every_reference_name():
+    """Every configuration name and kernel of the reference's table has a mirror, both in
+    seemps2_gb300.kernel_table and at the package top level."""
+    import seemps2_gb300 as sg
+    from seemps2_gb300 import kernel_table as kt
+
+    for name in REFERENCE_CONFIG + REFERENCE_KERNELS:
+        assert hasattr(kt, name), name
+        assert hasattr(sg, name), name
+    assert kt.active_backend() == "gb300"
+
+
+def test_select_svd_driver_validates_like_the_reference():
+    from seemps2_gb300 import _lib
+    from seemps2_gb300.kernel_table import _select_svd_driver
+
+    _select_svd_driver("gesvd")
+    assert _lib.load().sm_svd_driver() == 1
+    _select_svd_driver("gesdd")
+    assert _lib.load().sm_svd_driver() == 0
+    with pytest.raises(ValueError):
+        _select_svd_driver("dgesvj")

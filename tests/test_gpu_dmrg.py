@@ -114,3 +114,96 @@ def test_lanczos_lowest_eigenvalue(precision, bar):
         x = vec.cpu().numpy().reshape(-1)
         r = M @ x - ev * x
         assert np.linalg.norm(r) <= 1e-6 * abs(ev)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_mpo_environments_match_oracle(cplx):
+    rng = np.random.default_rng(21 + cplx)
+
+    def r(*s):
+        x = rng.normal(size=s)
+        return x + 1j * rng.normal(size=s) if cplx else x
+
+    for (a, j, d, c, e, b, f) in [(1, 2, 3, 1, 5, 1, 4), (9, 2, 12, 5, 5, 7, 10),
+                                  (64, 2, 48, 3, 4, 40, 56)]:
+        A, O, B = r(a, j, d), r(c, j, j, e), r(b, j, f)
+        rho = r(a, c, b)
+        got = dmrg.update_left_mpo_environment(rho, A, O, B).cpu().numpy()
+        ref = do.update_left_mpo_environment(rho, A, O, B)
+        assert np.allclose(got, ref, atol=1e-12 * np.abs(ref).max())
+        rho = r(d, e, f)
+        got = dmrg.update_right_mpo_environment(rho, A, O, B).cpu().numpy()
+        ref = do.update_right_mpo_environment(rho, A, O, B)
+        assert np.allclose(got, ref, atol=1e-12 * np.abs(ref).max())
+
+
+def _fixture(name):
+    import json
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    W = [z[f"W{i}"] for i in range(sum(1 for k in z.files if k.startswith("W")))]
+    return z, W, json.loads(bytes(z["meta"]).decode())["params"]
+
+
+def test_matvec_and_environments_match_reference_fixture():
+    """The reference's own QuadraticForm (HeisenbergHamiltonian(10).to_mpo(), a bond-8 state
+    centred at site 4): its L, H12, R and one two_site_operator matvec, against the
+    device's environments built from the same state and the device matvec."""
+    import seemps2_gb300 as sg
+
+    z, W, p = _fixture("dmrg_matvec_L10")
+    i = p["site"]
+    state = [z[f"A{k}"] for k in range(p["L"])]
+    out = dmrg.two_site_matvec(z["L"], z["H12"], z["R"], z["v"], "fp64").cpu().numpy()
+    assert np.allclose(out, z["out"], atol=1e-12 * np.abs(z["out"]).max())
+    psi = sg.CanonicalMPS(state, center=i, is_canonical=True)
+    QF = dmrg.QuadraticForm(sg.MPO(W), psi, start=i)
+    L, H12, R = QF.two_site_block(i)
+    assert np.allclose(L.cpu().numpy(), z["L"], atol=1e-12)
+    assert np.allclose(R.cpu().numpy(), z["R"], atol=1e-12)
+    assert np.allclose(H12.cpu().numpy(), z["H12"], atol=1e-14)
+
+
+def test_dmrg_matches_reference_run():
+    """Two DMRG sweeps of an L=10 Heisenberg chain from a seeded bond-4 guess (tolerance
+    1e-10, max bond 32): the energy after each sweep within 1e-9 of the reference's run,
+    the same bond dimensions, and the final state's overlap with the reference's to 1e-8."""
+    import importlib.util
+    import os
+
+    import seemps2_gb300 as sg
+
+    z, W, p = _fixture("dmrg_run_L10")
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    guess = mg.make_dmrg_inputs(p)
+    st = sg.DEFAULT_STRATEGY.replace(tolerance=p["tol"], max_bond_dimension=p["maxchi"])
+    res = dmrg.dmrg(sg.MPO(W), guess=sg.MPS(guess), maxiter=p["maxiter"], tol=1e-14, strategy=st)
+    traj = np.array(res.trajectory)
+    assert traj.shape == z["trajectory"].shape
+    assert np.max(np.abs(traj - z["trajectory"])) <= 1e-9 * max(1.0, abs(z["energy"]))
+    assert abs(res.energy - float(z["energy"])) <= 1e-9 * max(1.0, abs(z["energy"]))
+    assert res.state.bond_dimensions() == z["bonds"].tolist()
+    v = res.state.to_vector().cpu().numpy().reshape(-1)
+    ref = z["vector"].reshape(-1)
+    ov = abs(np.vdot(ref, v)) / (np.linalg.norm(ref) * np.linalg.norm(v))
+    assert 1.0 - ov <= 1e-8, 1.0 - ov
+
+
+@pytest.mark.parametrize("precision", ["bf16", "tf32x3"])
+def test_dmrg_reduced_precision_matches_fp64(precision):
+    """The reduced-precision Lanczos (BF16 or 3xTF32 matvecs, FP64 polish of each eigenpair)
+    reaches the FP64 run's energy."""
+    import seemps2_gb300 as sg
+
+    z, W, p = _fixture("dmrg_run_L10")
+    rng = np.random.default_rng(7)
+    guess = so.random_mps(2, p["L"], 4, rng)
+    st = sg.DEFAULT_STRATEGY.replace(tolerance=1e-10, max_bond_dimension=32)
+    e64 = dmrg.dmrg(sg.MPO(W), guess=sg.MPS(guess), maxiter=2, tol=1e-14, strategy=st).energy
+    er = dmrg.dmrg(sg.MPO(W), guess=sg.MPS(guess), maxiter=2, tol=1e-14, strategy=st,
+                   precision=precision).energy
+    assert abs(er - e64) <= 1e-8 * abs(e64), (er, e64)

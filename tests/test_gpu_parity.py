@@ -35,7 +35,7 @@ def run_gpu(p, mps, mpo):
 
 @pytest.mark.parametrize("name", CASE_NAMES)
 def test_parity_with_reference_run(name):
-    p, mps, mpo, g, same = load_case(name)
+    p, mps, mpo, g, _ = load_case(name)
     out, tr = run_gpu(p, mps, mpo)
     rec = so.Recorder()
     res, _ = run_oracle(p, mps, mpo, rec)
@@ -43,10 +43,18 @@ def test_parity_with_reference_run(name):
     assert tr.ranks == [sp.rank for sp in rec.splits]
     for s_gpu, sp in zip(tr.s, rec.splits):
         sv_close(s_gpu, sp.s, 1e-10)
-    if same:  # the fixture was made from these very inputs: compare with the reference too
-        assert tr.ranks == g["split_rank"].tolist()
-        assert out.bond_dimensions() == g["bonds"].tolist()
-        assert out.center == int(g["center"])
+    # the reference's own run (the fixture; its inputs are regenerated from the seed, so on
+    # another platform they may differ in the last bits, which these tolerances absorb):
+    # identical kept ranks at every split, singular values within 1e-10 s_max (large
+    # fixtures store each split's values up to the kept rank + 16), same bonds and centre
+    assert tr.ranks == g["split_rank"].tolist()
+    assert [len(s) for s in tr.s] == g["split_full_len"].tolist()
+    for s_gpu, s_ref in zip(tr.s, g["splits_s"]):
+        sv_close(np.asarray(s_gpu)[: len(s_ref)], s_ref, 1e-10)
+    assert out.bond_dimensions() == g["bonds"].tolist()
+    assert out.center == int(g["center"])
+    e1, e2 = out.error() ** 2, float(g["error"]) ** 2
+    assert abs(e1 - e2) <= 1e-13 + 1e-8 * e2
     assert out.bond_dimensions() == [A.shape[0] for A in res.tensors] + [1]
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-12, fe

@@ -60,10 +60,11 @@ def test_oracle_matches_reference_run(name):
     assert res.center == int(g["center"])
     # every split: identical kept rank, singular values within 1e-10 of s_max
     assert [sp.rank for sp in rec.splits] == g["split_rank"].tolist()
-    for sp, s_ref in zip(rec.splits, g["splits_s"]):
-        assert len(sp.s) == len(s_ref)
+    # (large fixtures store each split's values up to the kept rank + 16)
+    for sp, s_ref, n_full in zip(rec.splits, g["splits_s"], g["split_full_len"]):
+        assert len(sp.s) == n_full
         smax = max(float(s_ref[0]), 1e-300)
-        assert np.max(np.abs(sp.s - s_ref)) <= 1e-10 * smax
+        assert np.max(np.abs(sp.s[: len(s_ref)] - s_ref)) <= 1e-10 * smax
     # error bound: its square is the stable quantity (see make_golden.py)
     e1, e2 = res.error ** 2, float(g["error"]) ** 2
     assert abs(e1 - e2) <= 1e-13 + 1e-8 * e2
@@ -73,3 +74,57 @@ def test_oracle_matches_reference_run(name):
         v = so.to_vector(res.tensors)
         ref = g["vector"]
         assert np.linalg.norm(v - ref) <= 1e-9 * np.linalg.norm(ref)
+
+
+def _dmrg_fixture(name):
+    import json
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    W = [z[f"W{i}"] for i in range(sum(1 for k in z.files if k.startswith("W")))]
+    return z, W, json.loads(bytes(z["meta"]).decode())["params"]
+
+
+def test_dmrg_matvec_oracle_matches_reference():
+    """The oracle's environments and two-site matvec against the reference's QuadraticForm
+    on HeisenbergHamiltonian(10).to_mpo() (fixture made by tests/golden/make_golden.py)."""
+    from oracle import dmrg_oracle as do
+
+    z, W, p = _dmrg_fixture("dmrg_matvec_L10")
+    i = p["site"]
+    state = [z[f"A{k}"] for k in range(p["L"])]
+    L = do.begin_mpo_environment()
+    for k in range(i):
+        L = do.update_left_mpo_environment(L, state[k], W[k], state[k])
+    R = do.begin_mpo_environment()
+    for k in range(p["L"] - 1, i + 1, -1):
+        R = do.update_right_mpo_environment(R, state[k], W[k], state[k])
+    assert np.allclose(L, z["L"], atol=1e-13)
+    assert np.allclose(R, z["R"], atol=1e-13)
+    assert np.allclose(do.two_site_hamiltonian(W[i], W[i + 1]), z["H12"], atol=1e-15)
+    out = do.two_site_matvec(z["L"], z["H12"], z["R"], z["v"])
+    assert np.allclose(out, z["out"], atol=1e-13 * np.abs(z["out"]).max())
+
+
+def test_dmrg_oracle_matches_reference_run():
+    """The oracle's DMRG driver (scipy eigsh, as the reference) reproduces the reference's
+    two-sweep run: energies per sweep, bonds and the final state."""
+    import importlib.util
+    import os
+
+    from oracle import dmrg_oracle as do
+
+    z, W, p = _dmrg_fixture("dmrg_run_L10")
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    guess = mg.make_dmrg_inputs(p)
+    st = so.DEFAULT_STRATEGY.replace(tolerance=p["tol"], max_bond_dimension=p["maxchi"])
+    energy, state, traj, _, _, _ = do.dmrg(W, guess, maxiter=p["maxiter"], tol=1e-14, strategy=st)
+    assert np.max(np.abs(np.array(traj) - z["trajectory"])) <= 1e-9 * max(1.0, abs(energy))
+    assert abs(energy - float(z["energy"])) <= 1e-9
+    assert [A.shape[0] for A in state] + [1] == z["bonds"].tolist()
+    v = so.to_vector(state)
+    ref = z["vector"].reshape(-1)
+    assert 1.0 - abs(np.vdot(ref, v)) / (np.linalg.norm(ref) * np.linalg.norm(v)) <= 1e-8
