@@ -453,6 +453,85 @@ def run_dmrg_matvec(args):
     print(json.dumps(out), flush=True)
 
 
+def make_dmrg_workload(L: int, chi: int, seed: int = SEED + 11):
+    """The DMRG configuration's inputs: the spin-1/2 Heisenberg chain's MPO (J = 1, open
+    boundaries, bond 5) as the reference's HeisenbergHamiltonian(L).to_mpo() builds it
+    (recorded from the reference in tests/golden/heisenberg_mpo_L100.npz; its bulk tensor
+    repeats, so shorter chains take the first and last tensors around L - 2 bulk ones),
+    and a random float64 guess of bond chi (i.i.d. normal cores, each scaled to unit
+    Frobenius norm so that the chain's norm stays in range; the driver normalises it)."""
+    from oracle import seemps_oracle as so
+
+    z = np.load(os.path.join(ROOT, "tests", "golden", "heisenberg_mpo_L100.npz"))
+    W100 = [z[f"W{i}"] for i in range(100)]
+    W = [W100[0]] + [W100[1]] * (L - 2) + [W100[99]] if L != 100 else W100
+    rng = np.random.default_rng(seed)
+    guess = [A / np.linalg.norm(A) for A in so.random_mps(2, L, chi, rng)]
+    return W, guess
+
+
+def run_dmrg(args):
+    """The DMRG configuration end to end: two two-site DMRG sweeps of the L-site Heisenberg
+    chain from a random bond-chi guess, truncation tolerance 1e-10, max bond chi.  Forms:
+    "fp64" (FP64 matvecs and FP64 splits, the reference's arithmetic) and "bf16" (the
+    precision pattern: BF16 tensor-core matvecs with FP32 accumulation for the Krylov
+    basis, re-orthogonalised in FP64, each eigenpair polished with FP64-accurate
+    tensor-core matvecs; mixed-precision splits with FP64 truncation decisions).  Reports
+    sweeps/s, ms per two-site step and the energies.  The eigensolver tolerance is the
+    reference's default (tol_eigs = tol = 1e-10).  The CPU oracle (scipy eigsh, NumPy, all
+    host cores) is timed on the first steps of the first sweep."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import seemps2_gb300 as sg
+    from oracle import dmrg_oracle as do
+    from oracle import seemps_oracle as so
+    from seemps2_gb300 import _lib, dmrg
+
+    L, chi = args.dmrg_sites, args.dmrg_chi
+    W, guess = make_dmrg_workload(L, chi)
+    st = sg.DEFAULT_STRATEGY.replace(tolerance=1e-10, max_bond_dimension=chi)
+    H = sg.MPO(W)
+    out = {"workload": f"two-site DMRG, Heisenberg chain L={L} (MPO bond 5, the reference's "
+                       f"to_mpo), random guess of bond {chi}, tolerance 1e-10, max bond {chi}, "
+                       "2 sweeps", "sweeps": 2}
+    for form, prec, split in (("fp64", "fp64", "fp64"), ("bf16", "bf16", "mixed")):
+        sg.set_precision(split)
+        # warm-up on a short chain (kernels loaded, buffers sized)
+        Ws, gs = make_dmrg_workload(6, 8)
+        dmrg.dmrg(sg.MPO(Ws), guess=sg.MPS(gs), maxiter=1, strategy=st, precision=prec)
+        torch.cuda.synchronize()
+        _lib.stats_reset()
+        t0 = time.perf_counter()
+        res = dmrg.dmrg(H, guess=sg.MPS(guess), maxiter=2, strategy=st, precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        stt = _lib.stats_read()
+        nsw = len(res.trajectory) - 1
+        out[form] = {"s": dt, "sweeps_per_s": nsw / dt, "ms_per_step": 1e3 * dt / (nsw * (L - 1)),
+                     "trajectory": res.trajectory, "variances": res.variances,
+                     "bonds_max": max(res.state.bond_dimensions()),
+                     "launches": stt["launches"], "mixed_splits": stt["mixed_splits"],
+                     "mixed_fallbacks": stt["mixed_fallbacks"]}
+    sg.set_precision("fp64")
+    out["bf16"]["energy_diff_vs_fp64"] = out["bf16"]["trajectory"][-1] - out["fp64"]["trajectory"][-1]
+    if not args.no_cpu:
+        nsteps = args.dmrg_cpu_steps
+        t0 = time.perf_counter()
+        do.dmrg(W, guess, maxiter=1,
+                strategy=so.DEFAULT_STRATEGY.replace(tolerance=1e-10, max_bond_dimension=chi),
+                max_steps=nsteps)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "kind": "port", "cores": os.cpu_count(),
+            "sample": f"the oracle's canonical form, environments and first {nsteps} two-site "
+                      f"steps of sweep 1 ({dt:.1f} s), scaled to a sweep of {L - 1} steps",
+            "s_per_step": dt / nsteps, "sweeps_per_s": nsteps / (dt * (L - 1))}
+    print(json.dumps(out), flush=True)
+
+
 def run_gemm_case(args):
     """One real M x N x K product (op N, N) timed with CUDA events: the FP64 SIMT
     GEMM, the tensor-core 3xTF32 GEMM (FP32 accuracy) and the FP64-accurate
@@ -531,6 +610,12 @@ def main():
     ap.add_argument("--gemm-case", type=int, nargs=3, metavar=("M", "N", "K"),
                     help="time one real M x N x K product on the tensor cores (3xTF32) and as "
                          "the FP64 GEMM, and exit")
+    ap.add_argument("--dmrg", action="store_true",
+                    help="two DMRG sweeps of the Heisenberg chain (FP64 and the BF16 pattern), "
+                         "sweeps/s and energies, and exit")
+    ap.add_argument("--dmrg-sites", type=int, default=100)
+    ap.add_argument("--dmrg-chi", type=int, default=256)
+    ap.add_argument("--dmrg-cpu-steps", type=int, default=8)
     ap.add_argument("--dmrg-matvec", action="store_true",
                     help="time the DMRG two-site matvec (chi 256, MPO bond 5) per precision and exit")
     ap.add_argument("--batch", action="store_true",
@@ -548,6 +633,8 @@ def main():
         return run_batch(args)
     if args.dmrg_matvec:
         return run_dmrg_matvec(args)
+    if args.dmrg:
+        return run_dmrg(args)
     if args.impl == "reference":
         return run_reference(args)
 

@@ -182,8 +182,11 @@ int sm_gemm_ex(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
  * op(B), cut into 8 slices of 7-bit integers (exact in BF16) and multiplied
  * slice by slice with tcgen05 (Ozaki, Ogita, Oishi and Rump, Numer. Algorithms
  * 59, 2012), exact FP32 accumulation over chunks of 256 and FP64 across
- * chunks; the error is that of an FP64 GEMM.  Other shapes and complex
- * operands run the FP64 SIMT kernel.  The mixed precision forms route their
+ * chunks; the error is that of an FP64 GEMM.  Complex operands are held as
+ * split real planes (re, im, re + im) and multiplied with three real products
+ * of this kind (T1 = Ar Br, T2 = Ai Bi, T3 = (Ar+Ai)(Br+Bi); C = T1 - T2 +
+ * i (T3 - T1 - T2)).  Shapes below the tensor-core threshold run the FP64 SIMT
+ * kernel.  The mixed precision forms route their
  * FP64 products here (sm_ctx_set_fp64_products). */
 int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
                   const void* A, int lda, const void* B, int ldb, void* C, int ldc,
@@ -204,8 +207,9 @@ int sm_ctx_set_fp64_products(void* ctx, int tensor_cores);
 /* The same product at FP32 accuracy: the contractions of the mixed precision
  * forms (sm_ctx_set_contraction_bits(ctx, 32)).  Real operands with
  * M, N >= 64, K >= 32 and at least 4 Mi multiply-adds run 3xTF32 on the
- * tensor cores (tcgen05, FP32 accumulation); other shapes and complex
- * operands run an FP32 SIMT kernel.  No reference counterpart (the reference
+ * tensor cores (tcgen05, FP32 accumulation); complex operands of those shapes
+ * as three real 3xTF32 products on split re / im / re+im planes (the 3M form);
+ * other shapes run an FP32 SIMT kernel.  No reference counterpart (the reference
  * contracts in FP64). */
 int sm_gemm_f32(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
                 const void* A, int lda, const void* B, int ldb, void* C, int ldc,

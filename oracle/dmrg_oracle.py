@@ -118,12 +118,14 @@ def _energy_and_variance(W, state, center):
     return energy, abs(so.norm_squared(hpsi) - energy * energy)
 
 
-def dmrg(W, guess, maxiter=20, tol=1e-10, tol_up=None, tol_eigs=None, strategy=None):
+def dmrg(W, guess, maxiter=20, tol=1e-10, tol_up=None, tol_eigs=None, strategy=None,
+         max_steps=None):
     """optimization/dmrg.py:76-199 on lists of tensors: guess canonicalised at site 0 and
     normalised, sweeps of eigsh(which="SA") on the two-site operators from the current
     two-site tensor, left/right splits with the strategy (normalize=True), energy and
     variance after each sweep, the same stop rule.  Returns (best energy, best state,
-    trajectory, variances, converged, sweeps)."""
+    trajectory, variances, converged, sweeps).  ``max_steps`` (timing samples only) stops
+    after that many two-site steps."""
     import scipy.sparse.linalg as sla
 
     from oracle import seemps_oracle as so
@@ -144,10 +146,14 @@ def dmrg(W, guess, maxiter=20, tol=1e-10, tol_up=None, tol_eigs=None, strategy=N
     best = (energy, [A.copy() for A in state])
     trajectory, variances = [energy], [variance]
     direction, last_energy, converged, sweeps = +1, energy, False, 0
+    steps = 0
     for sweep in range(1, maxiter + 1):
         sweeps = sweep
         sites = range(size - 1) if direction > 0 else range(size - 2, -1, -1)
         for i in sites:
+            if max_steps is not None and steps >= max_steps:
+                return best[0], state, trajectory, variances, False, sweeps
+            steps += 1
             L, R = left[i], right[i + 1]
             H = two_site_hamiltonian(W[i], W[i + 1])
             v = np.tensordot(state[i], state[i + 1], axes=1)

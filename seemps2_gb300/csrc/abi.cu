@@ -443,6 +443,13 @@ int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K, c
                      0.0, (double*)C, ldc));
     return tc_status_check(c, s);
   }
+  if (dtype == SM_COMPLEX128 && M && N && K && gemm_cplx_oz_eligible(M, N, K)) {
+    c.stats.gemm_oz_launches += 3;
+    c.stats.gemm_oz_flops += 6.0 * M * N * K;
+    SM_CHECK(gemm_cplx_3m(c, s, opA, opB, M, N, K, cplx{1.0, 0.0}, (const cplx*)A, lda,
+                          (const cplx*)B, ldb, cplx{0.0, 0.0}, (cplx*)C, ldc, true));
+    return tc_status_check(c, s);
+  }
   return sm_gemm(ctx, dtype, opA, opB, M, N, K, A, lda, B, ldb, C, ldc, stream);
 }
 

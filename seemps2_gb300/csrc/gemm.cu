@@ -414,6 +414,24 @@ int gemm_ctx_sel(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int 
       }
       return SM_OK;
     }
+  } else {
+    // mixed forms, complex operands: three real FP64-accurate products (3M)
+    if (allow_tc && ctx.precision != SM_PRECISION_FP64 && ctx.fp64_tc &&
+        gemm_cplx_oz_eligible(M, N, K)) {
+      ctx.stats.gemm_oz_launches += 3;
+      ctx.stats.gemm_oz_flops += 6.0 * M * N * K;
+      if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+      SM_CHECK(gemm_cplx_3m(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc,
+                            true));
+      if (ctx.timing) {
+        SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+        SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
+        float ms = 0.f;
+        SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+        ctx.stats.gemm_oz_ms += ms;
+      }
+      return SM_OK;
+    }
   }
   ctx.stats.gemm_launches += 1;
   ctx.stats.gemm_flops += 2.0 * M * N * K * (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
@@ -483,6 +501,24 @@ int gemm_ctx_f32(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int 
       SM_CHECK(gemm_tc(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc));
       ctx.stats.gemm_tc_launches += 1;
       ctx.stats.gemm_tc_flops += 2.0 * M * N * K;
+      if (ctx.timing) {
+        SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+        SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));
+        float ms = 0.f;
+        SM_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+        ctx.stats.gemm32_ms += ms;
+        ctx.stats.gemm_tc_ms += ms;
+      }
+      return SM_OK;
+    }
+  } else {
+    // complex operands: three real 3xTF32 products on split planes (3M)
+    if (gemm_cplx_tc_eligible(M, N, K)) {
+      if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+      SM_CHECK(gemm_cplx_3m(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc,
+                            false));
+      ctx.stats.gemm_tc_launches += 3;
+      ctx.stats.gemm_tc_flops += 6.0 * M * N * K;
       if (ctx.timing) {
         SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
         SM_CUDA_CHECK(cudaEventSynchronize(ctx.ev1));

@@ -180,6 +180,15 @@ bool gemm_oz_eligible(int M, int N, int K);
 int gemm_oz(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, double alpha,
             const double* A, int lda, const double* B, int ldb, double beta, double* C, int ldc);
 
+// --- gemm_cplx.cu -------------------------------------------------------------
+// Complex product as three real products (3M) on split re / im / re+im planes:
+// on the 3xTF32 tensor-core GEMM, or the FP64-accurate one (fp64_accurate).
+// Callers check gemm_cplx_tc_eligible / gemm_cplx_oz_eligible on (M, N, K).
+bool gemm_cplx_tc_eligible(int M, int N, int K);
+bool gemm_cplx_oz_eligible(int M, int N, int K);
+int gemm_cplx_3m(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, cplx alpha,
+                 const cplx* A, int lda, const cplx* B, int ldb, cplx beta, cplx* C, int ldc,
+                 bool fp64_accurate);
 // --- dmrg.cu -----------------------------------------------------------------
 template <typename T>
 int two_site_matvec(Ctx& ctx, cudaStream_t st, int a, int c, int b, int p1, int p2, int e, int g,

@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cfloat>
+#include <climits>
 #include <cmath>
 
 #include "kernels.cuh"
@@ -432,8 +433,23 @@ __global__ void __launch_bounds__(NT) k_jacobi(T* Wx, int ld, int k, int l, int 
 }
 
 // s_i = |w_i|, one warp per row
+// The FP64 splits square entries (row norms, overlaps, Householder norms) and
+// square those again (the Jacobi's g^2 vs tol^2 a b test), which under- or
+// overflows for matrices whose entries are far from 1 (the canonical form of a
+// long random chain carries a scale of 1e-120 and below).  So, as LAPACK
+// rescales its input, the split runs on the matrix times 2^-e, e the exponent
+// of its largest entry: exact, so singular values and vectors scale back
+// exactly.  k_max_exp takes e with an atomic max over the blocks (the word is
+// set to 0x80808080, below every exponent, beforehand); scale_exp reads it
+// back (0 for an all-zero or non-finite matrix, which the split reports).
+__device__ __forceinline__ int scale_exp(const int* wexp) {
+  const int e = *wexp;
+  return (e < -1100 || e > 1100) ? 0 : e;
+}
+
 template <typename T>
-__global__ void k_row_norms(const T* W, int ldw, int k, int l, double* nrm, int squared) {
+__global__ void k_row_norms(const T* W, int ldw, int k, int l, double* nrm, int squared,
+                            const int* wexp = nullptr) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x % 32;
   if (warp >= k) return;
@@ -442,7 +458,53 @@ __global__ void k_row_norms(const T* W, int ldw, int k, int l, double* nrm, int 
   for (int x = lane; x < l; x += 32) a += S<T>::abs2(ldcg(w + x));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-  if (lane == 0) nrm[warp] = squared ? a : sqrt(a);
+  // rows scaled by 2^-e (see k_max_exp): the norm of the unscaled row
+  if (lane == 0) nrm[warp] = squared ? a : (wexp ? ldexp(sqrt(a), scale_exp(wexp)) : sqrt(a));
+}
+
+template <typename T>
+__global__ void k_max_exp(const T* __restrict__ X, int rows, int cols, int ldx, int* e_out) {
+  int best = INT_MIN;
+  const size_t total = (size_t)rows * cols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const T v = X[(i / cols) * ldx + (i % cols)];
+    double m;
+    if constexpr (sizeof(T) == sizeof(double)) m = fabs((double)S<T>::real(v));
+    else m = fmax(fabs(v.re), fabs(v.im));
+    if (m > 0.0 && isfinite(m)) best = max(best, ilogb(m));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0 && best != INT_MIN) atomicMax(e_out, best);
+}
+
+template <typename T>
+__global__ void k_scale_exp(T* __restrict__ X, int rows, int cols, int ldx,
+                            const int* __restrict__ wexp) {
+  const int e = -scale_exp(wexp);
+  if (e == 0) return;
+  const size_t total = (size_t)rows * cols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    T& v = X[(i / cols) * ldx + (i % cols)];
+    if constexpr (sizeof(T) == sizeof(double)) v = ldexp((double)S<T>::real(v), e);
+    else v = T{ldexp(v.re, e), ldexp(v.im, e)};
+  }
+}
+
+// Scale the rows x cols block of X (leading dimension ldx) by 2^-e, e the
+// exponent of its largest entry, kept in *wexp for the way back.
+template <typename T>
+int prescale(cudaStream_t st, T* X, int rows, int cols, int ldx, int* wexp) {
+  const size_t total = (size_t)rows * cols;
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>((total + 255) / 256, 1024));
+  SM_CUDA_CHECK(cudaMemsetAsync(wexp, 0x80, sizeof(int), st));
+  k_max_exp<T><<<blocks, 256, 0, st>>>(X, rows, cols, ldx, wexp);
+  k_scale_exp<T><<<blocks, 256, 0, st>>>(X, rows, cols, ldx, wexp);
+  note_launch(2);
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
 }
 
 // The reference truncation rules, executed by one thread.  Products and sums
@@ -584,7 +646,10 @@ template <typename T>
 __global__ void k_emit(int wide, int m, int n, int D, const T* __restrict__ W, int ldw,
                        const T* __restrict__ X, int ldx, const int* __restrict__ perm,
                        const double* __restrict__ s, int left_mode, T* __restrict__ left,
-                       int right_mode, T* __restrict__ right) {
+                       int right_mode, T* __restrict__ right, const int* wexp = nullptr) {
+  // W's rows carry the prescale 2^-e (X's do not): normalising a W row takes
+  // the singular value times 2^-e
+  const int we = wexp ? -scale_exp(wexp) : 0;
   const size_t nl = left_mode ? (size_t)m * D : 0;
   const size_t nr = right_mode ? (size_t)D * n : 0;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nl + nr;
@@ -599,7 +664,8 @@ __global__ void k_emit(int wide, int m, int n, int D, const T* __restrict__ W, i
         if (left_mode == OUT_US) v = S<T>::scale(v, sj);
       } else {
         v = W[(size_t)pj * ldw + i];
-        if (left_mode == OUT_U) v = sj > 0.0 ? S<T>::scale(v, 1.0 / sj) : S<T>::zero();
+        if (left_mode == OUT_U) v = sj > 0.0 ? S<T>::scale(v, 1.0 / ldexp(sj, we)) : S<T>::zero();
+        else if (we) v = S<T>::scale(v, ldexp(1.0, -we));  // U s: undo the prescale
       }
       left[e] = v;
     } else {
@@ -610,7 +676,8 @@ __global__ void k_emit(int wide, int m, int n, int D, const T* __restrict__ W, i
       T v;
       if (wide) {
         v = W[(size_t)pj * ldw + x];
-        if (right_mode == OUT_VT) v = sj > 0.0 ? S<T>::scale(v, 1.0 / sj) : S<T>::zero();
+        if (right_mode == OUT_VT) v = sj > 0.0 ? S<T>::scale(v, 1.0 / ldexp(sj, we)) : S<T>::zero();
+        else if (we) v = S<T>::scale(v, ldexp(1.0, -we));  // s V: undo the prescale
       } else {
         v = S<T>::conj(X[(size_t)pj * ldx + x]);
         if (right_mode == OUT_SVT) v = S<T>::scale(v, sj);
@@ -640,10 +707,8 @@ static void deflation(const sm_strategy& s, int k, double* rel, double* abs_) {
   if (s.method == SM_RELATIVE_NORM_SQUARED_ERROR) *rel = std::min(1e-24, 1e-6 * s.tolerance) / k;
   else if (s.method == SM_RELATIVE_SINGULAR_VALUE)
     *rel = std::min(1e-24, 1e-4 * s.tolerance * s.tolerance) / k;
-  else if (s.method == SM_ABSOLUTE_SINGULAR_VALUE) {
-    *rel = 1e-24 / k;
-    *abs_ = 1e-4 * s.tolerance * s.tolerance;
-  }
+  else if (s.method == SM_ABSOLUTE_SINGULAR_VALUE)
+    *rel = 1e-24 / k;  // no absolute threshold: the iteration runs on prescaled values
 }
 
 template <typename T, int E>
@@ -941,12 +1006,15 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(ctx.scratch("svd.ctl", 1, &ctl));
   SM_CHECK(ctx.scratch("svd.qctl", 1, &qctl));
   SM_CHECK(ctx.scratch("svd.res", 1, &res));
-  // Wt = W^T (l x kw): A itself for U, A^T for V
+  int* wexp;
+  SM_CHECK(ctx.scratch("svd.wexp", 1, &wexp));
+  // Wt = W^T (l x kw): A itself for U, A^T for V; then scaled to O(1) entries
   if (want_u) {
     SM_CUDA_CHECK(cudaMemcpyAsync(Wt, A, sizeof(T) * (size_t)m * n, cudaMemcpyDeviceToDevice, st));
   } else {
     SM_CHECK(transpose<T>(st, m, n, A, n, Wt, m));
   }
+  SM_CHECK(prescale<T>(st, Wt, l, kw, kw, wexp));
   double drel, dabs;
   deflation(strat, k, &drel, &dabs);
   // rank-revealing QR preconditioner: W = Q R, R has k rows
@@ -998,7 +1066,7 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     ctx.stats.jacobi_flops += (4.0 * std::max(m, n) * (double)k * k + 8.0 * (double)k * k * k) *
                               (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
   }
-  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
+  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0, wexp);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   SM_CHECK(sort_truncate(st, nrm, k, strat, perm, s_sorted, errors, ctl, res));
@@ -1063,14 +1131,14 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   if (want_u) {
     // U (m x D) = normalised rows of W^T; then S V (D x n) = U^H A
     k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(0, m, n, D, Wx, ld, Wx, ld, perm, s_sorted, OUT_U,
-                                                   iso_w, 0, oth_w);
+                                                   iso_w, 0, oth_w, wexp);
     note_launch();
     SM_CUDA_CHECK(cudaGetLastError());
     SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, D, n, m, one, iso_w, D, A, n, zero, oth_w, n));
   } else {
     // V (D x n) = normalised rows of W; then U S (m x D) = A V^H
     k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(1, m, n, D, Wx, ld, Wx, ld, perm, s_sorted, 0,
-                                                   oth_w, OUT_VT, iso_w);
+                                                   oth_w, OUT_VT, iso_w, wexp);
     note_launch();
     SM_CUDA_CHECK(cudaGetLastError());
     SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, m, D, n, one, A, n, iso_w, n, zero, oth_w, D));
@@ -1696,6 +1764,8 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
   SM_CHECK(ctx.scratch("svd.perm", (size_t)k, &perm));
   SM_CHECK(ctx.scratch("svd.ctl", 1, &ctl));
   SM_CHECK(ctx.scratch("svd.res", 1, &res));
+  int* wexp;
+  SM_CHECK(ctx.scratch("svd.wexp", 1, &wexp));
 
   if (wide) {
     SM_CUDA_CHECK(cudaMemcpy2DAsync(Wx, sizeof(T) * ld, A, sizeof(T) * n, sizeof(T) * n, m,
@@ -1703,6 +1773,7 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
   } else {
     SM_CHECK(transpose<T>(st, m, n, A, n, Wx, ld));
   }
+  SM_CHECK(prescale<T>(st, Wx, k, l, ld, wexp));
   {
     const size_t tot = (size_t)k * k;
     const int blocks = (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, 4096));
@@ -1740,7 +1811,7 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
     ctx.stats.jacobi_flops += (4.0 * l * (double)k * k + 8.0 * (double)k * k * k) *
                               (sizeof(T) == sizeof(double) ? 1.0 : 4.0);
   }
-  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
+  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0, wexp);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   SM_CHECK(sort_truncate(st, nrm, k, strat, perm, s_sorted, errors, ctl, res));
@@ -1786,7 +1857,8 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
     const size_t total = (left_mode ? (size_t)m * D : 0) + (right_mode ? (size_t)D * n : 0);
     const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
     k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(wide, m, n, D, Wx, ld, Wx + l, ld, perm,
-                                                   s_sorted, left_mode, left, right_mode, right);
+                                                   s_sorted, left_mode, left, right_mode, right,
+                                                   wexp);
                                                    note_launch();
     SM_CUDA_CHECK(cudaGetLastError());
   }
@@ -1944,6 +2016,7 @@ int noalloc_attempt(cudaStream_t st, const T* A, int m, int n, const sm_strategy
       reinterpret_cast<unsigned char*>(perm) + ((kNoAllocMaxDim * sizeof(int) + 255) & ~size_t(255)));
   SplitResult* res = reinterpret_cast<SplitResult*>(reinterpret_cast<unsigned char*>(ctl) + 256);
   int* act = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(res) + 256);
+  int* wexp = act + kNoAllocMaxDim;
 
   if (wide) {
     SM_CUDA_CHECK(cudaMemcpy2DAsync(Wx, sizeof(T) * ld, A, sizeof(T) * n, sizeof(T) * n, m,
@@ -1951,6 +2024,7 @@ int noalloc_attempt(cudaStream_t st, const T* A, int m, int n, const sm_strategy
   } else {
     SM_CHECK(transpose<T>(st, m, n, A, n, Wx, ld));
   }
+  SM_CHECK(prescale<T>(st, Wx, k, l, ld, wexp));
   {
     const size_t tot = (size_t)k * k;
     const int blocks = (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, 4096));
@@ -1975,7 +2049,7 @@ int noalloc_attempt(cudaStream_t st, const T* A, int m, int n, const sm_strategy
     SM_CHECK(run_jacobi_noalloc<T>(st, Wx, ld, k, l, tol * tol, use_floor ? 1 : 0, drel, dabs, nrm,
                                    nrm0, act, ctl, one_cta));
   }
-  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0);
+  k_row_norms<T><<<(k + 7) / 8, 256, 0, st>>>(Wx, ld, k, l, nrm, 0, wexp);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   SM_CHECK(sort_truncate(st, nrm, k, strat, perm, s_sorted, errors, ctl, res));
@@ -1994,7 +2068,7 @@ int noalloc_attempt(cudaStream_t st, const T* A, int m, int n, const sm_strategy
   const size_t total = (size_t)m * D + (size_t)D * n;
   const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
   k_emit<T><<<std::max(blocks, 1), 256, 0, st>>>(wide, m, n, D, Wx, ld, Wx + l, ld, perm, s_sorted,
-                                                 OUT_U, left, OUT_SVT, right);
+                                                 OUT_U, left, OUT_SVT, right, wexp);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   *D_out = D;

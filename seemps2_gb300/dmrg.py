@@ -159,16 +159,17 @@ def _lanczos_cycle(apply, x0, m: int):
 
 
 def lanczos_ground_state(L, H, R, v0, krylov: int = 30, precision: str = "fp64", tol: float = 0.0,
-                         restarts: int = 0, polish: int = 0):
+                         restarts: int = 0, polish: int = 0, polish_precision: str = "fp64tc"):
     """Lowest eigenpair of the (Hermitian, real) two-site operator from the start vector v0.
 
     Each cycle is ``krylov`` Lanczos steps (FP64 basis, full re-orthogonalisation) with the
     matvecs in ``precision``; up to ``restarts`` more cycles restart from the Ritz vector
     while the residual estimate is above ``tol`` |lambda| (scipy's eigsh, which the reference
     calls with this tol, stops on the same relative criterion; tol = 0 means rounding level).
-    For a reduced precision, ``polish`` > 0 then runs FP64 cycles of ``polish`` steps from
-    the result until the same criterion holds (or ``restarts`` is used up), so the pair
-    reaches FP64 accuracy with most matvecs at the reduced precision.  Returns (eigenvalue,
+    For a reduced precision, ``polish`` > 0 then runs cycles of ``polish`` steps with
+    FP64-accurate matvecs (``polish_precision``: "fp64tc", the FP64-accurate tensor-core
+    products, or "fp64") from the result until the same criterion holds (or ``restarts`` is
+    used up), so the pair reaches FP64 accuracy with most matvecs at the reduced precision.  Returns (eigenvalue,
     eigenvector as a device tensor shaped like v0, matvecs run)."""
     L, H, R = (as_device(t, False) for t in (L, H, R))
     x = as_device(v0, False)
@@ -182,11 +183,14 @@ def lanczos_ground_state(L, H, R, v0, krylov: int = 30, precision: str = "fp64",
             two_site_matvec(L, H, R, v, precision, out=out)
 
     def full(v, out):
-        two_site_matvec(L, H, R, v, "fp64", out=out)
+        two_site_matvec(L, H, R, v, polish_precision, out=out)
 
     total = 0
     lam = 0.0
-    for _ in range(1 + max(0, restarts)):
+    # a reduced-precision operator cannot resolve the residual below its own rounding:
+    # one cycle of it, then the FP64-accurate polish
+    cycles = 1 if (op is not None and polish > 0) else 1 + max(0, restarts)
+    for _ in range(cycles):
         lam, x, res, steps = _lanczos_cycle(reduced, x, krylov)
         total += steps
         if res <= thr * max(abs(lam), 1e-300) or steps < krylov:
@@ -327,7 +331,7 @@ class QuadraticForm:
         v = _contract_last_and_first(self.state[i], self.state[i + 1])
         lam, x, _ = lanczos_ground_state(L, H12, R, v, krylov=krylov, precision=precision,
                                          tol=tol_eigs, restarts=restarts,
-                                         polish=8 if precision in ("tf32x3", "bf16") else 0)
+                                         polish=12 if precision in ("tf32x3", "bf16") else 0)
         return lam, x
 
     def update_2site_right(self, AB, i: int, strategy: Strategy) -> None:

@@ -158,6 +158,34 @@ def test_two_site_splits_on_degenerate_spectra_keep_reference_ranks(cplx):
 
 
 @pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("e", [-480, -300, 0, 300, 505])
+def test_fp64_splits_are_scale_invariant(e, cplx):
+    """The FP64 splits give the same ranks and 2^e times the singular values for a matrix
+    scaled by 2^e, far beyond where squared entries (or their squares) under- or overflow:
+    the split runs on the matrix prescaled by a power of two, as LAPACK rescales."""
+    rng = np.random.default_rng(abs(e) + cplx)
+    s0 = np.concatenate([np.geomspace(1.0, 1e-9, 30), [1e-13] * 4])
+    A = _clustered_matrix(64, 48, cplx, list(s0), rng)
+    As = A * 2.0**e
+    _, s_ref, _ = so.svd(A)
+    U, s, V = (to_np(x) for x in sg._destructive_svd(As))
+    sv_close(s * 2.0**-e, s_ref, 1e-12)
+    assert np.allclose(U.conj().T @ U, np.eye(48), atol=1e-11)
+    st = sg.DEFAULT_STRATEGY.replace(tolerance=1e-10, max_bond_dimension=64)
+    ost = so.DEFAULT_STRATEGY.replace(tolerance=1e-10, max_bond_dimension=64)
+    for gpu_fn, ora_fn in [(sg._left_orth_2site, so.left_orth_2site),
+                           (sg._right_orth_2site, so.right_orth_2site)]:
+        L, R, err = gpu_fn(As.reshape(32, 2, 2, 24), st)
+        Lo, Ro, eo = ora_fn(A.reshape(32, 2, 2, 24), ost)
+        assert L.shape == Lo.shape and R.shape == Ro.shape
+        D = L.shape[-1]
+        rec = (to_np(L).reshape(-1, D) @ to_np(R).reshape(D, -1)) * 2.0**-e
+        reco = Lo.reshape(-1, D) @ Ro.reshape(D, -1)
+        assert np.allclose(rec, reco, atol=1e-12 * np.abs(A).max())
+        assert abs(err * 2.0**-e - eo) <= 1e-9 * max(1e-3, eo)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
 def test_two_site_splits_match_oracle(cplx):
     st = sg.DEFAULT_STRATEGY.replace(tolerance=1e-8, max_bond_dimension=20)
     ost = so.DEFAULT_STRATEGY.replace(tolerance=1e-8, max_bond_dimension=20)

@@ -163,3 +163,88 @@ def test_fp64_tensor_core_gemm_cancellation():
     err = np.max(np.abs(out - ref) / scale)
     assert err < 8 * np.sqrt(K) * 2.0**-53
     assert err <= 2 * max(np.max(np.abs(native - ref) / scale), np.sqrt(K) * 2.0**-53)
+
+
+def _gemm_c(fn, opA, opB, A, B, M, N, K):
+    Ad = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    Bd = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    Cd = torch.empty((M, N), dtype=torch.complex128, device="cuda")
+    _lib.check(getattr(_lib.load(), fn)(
+        _lib.context(), _lib.SM_COMPLEX128, OPS[opA], OPS[opB], M, N, K,
+        C.c_void_p(Ad.data_ptr()), A.shape[1], C.c_void_p(Bd.data_ptr()), B.shape[1],
+        C.c_void_p(Cd.data_ptr()), N, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    return Cd.cpu().numpy()
+
+
+def _cplx_case(M, N, K, opA, opB, seed, scaled=False):
+    rng = np.random.default_rng(seed)
+    Aop = rng.normal(size=(M, K)) + 1j * rng.normal(size=(M, K))
+    Bop = rng.normal(size=(K, N)) + 1j * rng.normal(size=(K, N))
+    if scaled:
+        Aop *= np.exp(rng.uniform(-18, 18, size=(M, 1)))
+        Bop *= np.exp(rng.uniform(-18, 18, size=(1, N)))
+    # the stored operands whose op() is Aop / Bop
+    stored = {"N": lambda x: x, "T": lambda x: x.T.copy(), "C": lambda x: x.conj().T.copy()}
+    return Aop, Bop, stored[opA](Aop), stored[opB](Bop)
+
+
+@pytest.mark.parametrize("opB", ["N", "T", "C"])
+@pytest.mark.parametrize("opA", ["N", "T", "C"])
+@pytest.mark.parametrize("M,N,K", [(256, 192, 320), (130, 70, 120)])
+def test_complex_tensor_core_gemm_3m(M, N, K, opA, opB):
+    """Complex products on split real planes as three real 3xTF32 tensor-core products (the 3M
+    form): relative Frobenius error against numpy's complex128 product below 4e-6, every op
+    pair, ragged shapes."""
+    Aop, Bop, A, B = _cplx_case(M, N, K, opA, opB, M + N + K + 3 * OPS[opA] + OPS[opB])
+    _lib.stats_reset()
+    out = _gemm_c("sm_gemm_f32", opA, opB, A, B, M, N, K)
+    assert _lib.stats_read()["gemm_tc_launches"] == 3
+    ref = Aop @ Bop
+    rel = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    assert rel < 4e-6, rel
+
+
+@pytest.mark.parametrize("opB", ["N", "T", "C"])
+@pytest.mark.parametrize("opA", ["N", "T", "C"])
+@pytest.mark.parametrize("M,N,K", [(128, 96, 256), (225, 100, 300)])
+def test_complex_fp64_tensor_core_gemm_3m(M, N, K, opA, opB):
+    """Complex products as three FP64-accurate real tensor-core products: error normalised by
+    |A||B| within 16 sqrt(K) u and within four times the FP64 SIMT complex GEMM's own error
+    (at least sqrt(K) u), rows and columns scaled over 1e-8 .. 1e8."""
+    Aop, Bop, A, B = _cplx_case(M, N, K, opA, opB, 7 * M + N + K + OPS[opA], scaled=True)
+    _lib.stats_reset()
+    out = _gemm_c("sm_gemm_f64tc", opA, opB, A, B, M, N, K)
+    assert _lib.stats_read()["gemm_oz_launches"] == 3
+    native = _gemm_c("sm_gemm", opA, opB, A, B, M, N, K)
+    ref = Aop @ Bop
+    scale = np.abs(Aop) @ np.abs(Bop)
+    err = np.max(np.abs(out - ref) / scale)
+    err_native = np.max(np.abs(native - ref) / scale)
+    assert err < 16 * np.sqrt(K) * 2.0**-53, err
+    assert err <= 4 * max(err_native, np.sqrt(K) * 2.0**-53), (err, err_native)
+
+
+def test_complex_mixed_form_uses_tensor_cores():
+    """The complex MPO.apply + simplify of the first configuration (n=20, chi=32, D=4,
+    complex128, tolerance 1e-10, max bond 64) in the mixed form with FP32 contractions: its
+    complex contractions run as 3M tensor-core products, and the result stays within 1e-10
+    fidelity of the FP64 oracle."""
+    rng = np.random.default_rng(102)
+    n, chi, D = 20, 32, 4
+    mps = so.random_mps(2, n, chi, rng, complex_=True)
+    mps = so.scale(mps, 1.0 / np.sqrt(so.norm_squared(mps)))
+    mpo = so.random_mpo(2, n, D, rng, complex_=True)
+    kw = dict(tolerance=1e-10, max_bond_dimension=64, max_sweeps=2)
+    st = sg.DEFAULT_STRATEGY.replace(**kw)
+    sg.set_precision("mixed", contractions="fp32")
+    _lib.stats_reset()
+    try:
+        out = sg.MPO(mpo, st).apply(sg.MPS(mps), strategy=st)
+        stats = _lib.stats_read()
+    finally:
+        sg.set_precision("fp64")
+    ref = so.mpo_apply(mpo, mps, so.DEFAULT_STRATEGY.replace(**kw))
+    assert stats["gemm_tc_launches"] > 0, stats
+    fe = so.fidelity_error(mps_np(out), ref.tensors)
+    assert fe < 1e-10, fe
