@@ -214,6 +214,8 @@ def workload_config(args):
             "n": args.n, "chi": args.chi, "mpo_bond": 3, "tolerance": 1e-12,
             "max_bond_dimension": args.chi, "sweeps_per_step": 2, "form": args.form,
             "rank_cap": [getattr(args, "cap_margin", 1.15), getattr(args, "cap_extra", 10)],
+            "learned_use": "range finder (rank + 10, %d power iterations)" % getattr(args, "rf_power", 0)
+            if getattr(args, "range_finder", False) else "QR cap",
             "contractions": getattr(args, "contractions", "fp32"),
             "l2": "flushed between timed steps (256 MB write); the product MPS is >256 MB",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
@@ -242,8 +244,12 @@ def run_split_case(args):
     AA = torch.from_numpy(np.ascontiguousarray(A.reshape(m // 2, 2, 2, n // 2))).cuda()
     st = sg.Strategy(tolerance=1e-12, max_bond_dimension=256)
     out = {"split_case": [m, n], "steps": args.steps}
-    for form in ("plain", "mixed"):
-        sg.set_precision("fp64" if form == "plain" else "mixed")
+    for form in ("plain", "mixed", "range_finder"):
+        if form == "range_finder":  # the learned form's range finder at rank 256 + 10
+            sg.set_precision("mixed+learned", range_finder=True, rank_hint=256,
+                             power_iters=args.rf_power)
+        else:
+            sg.set_precision("fp64" if form == "plain" else "mixed")
         for _ in range(max(1, args.warmup)):
             core._left_orth_2site(AA, st)
         torch.cuda.synchronize()
@@ -259,6 +265,9 @@ def run_split_case(args):
         out[form] = {"ms_per_split": e0.elapsed_time(e1) / args.steps, "D": int(U.shape[-1]),
                      "err": float(err), "launches_per_split": stt["launches"] / args.steps,
                      "mixed_fallbacks": stt["mixed_fallbacks"],
+                     "fallback_reasons": {k: stt[k] for k in (
+                         "mixed_fallback_cut", "mixed_fallback_fp32", "mixed_fallback_over",
+                         "mixed_fallback_unconverged", "mixed_cap_redone", "rf_splits")},
                      "cluster_qr_ms": stt["cluster_qr_ms"] / args.steps,
                      "cluster_jacobi_ms": stt["cluster_jacobi_ms"] / args.steps,
                      "jacobi_sweeps_per_split": stt["jacobi_sweeps"] / args.steps}
@@ -605,6 +614,11 @@ def main():
     ap.add_argument("--cap-margin", type=float, default=1.15,
                     help="learned cap of the FP32 QR: ceil(margin * predicted rank) + extra rows")
     ap.add_argument("--cap-extra", type=int, default=10)
+    ap.add_argument("--range-finder", action="store_true",
+                    help="mixed+learned: the predicted rank sizes a randomized range finder (rank + "
+                         "10 columns) instead of capping the FP32 QR")
+    ap.add_argument("--rf-power", type=int, default=0,
+                    help="subspace (power) iterations of the range finder")
     ap.add_argument("--split-case", type=int, nargs=2, metavar=("M", "N"),
                     help="time single M x N two-site splits in both precision modes and exit")
     ap.add_argument("--gemm-case", type=int, nargs=3, metavar=("M", "N", "K"),
@@ -715,14 +729,26 @@ def main():
         return {"value": psw * len(pt) / (sum(pt) / 1e3), "unit": "sweeps/s",
                 "ms_per_step": sum(pt) / len(pt)}
 
-    no_predictor = None
+    no_predictor = rf_form = None
     if args.form != "plain":
         plain = time_form("fp64")
     if args.form == "mixed+learned":
-        # the same mixed form without the rank predictor: what the learned cap gains
+        # the same mixed form without the rank predictor: what the learned part gains
         no_predictor = time_form("mixed", contractions=args.contractions)
+        # the other use of the predicted rank: sizing a randomized range finder
+        _lib.stats_reset(timing=False)
+        rf_form = time_form("mixed+learned", contractions=args.contractions,
+                            range_finder=not args.range_finder, power_iters=args.rf_power)
+        s_rf = _lib.stats_read()
+        kk = max(1, args.steps + 1)
+        rf_form.update({"range_finder": not args.range_finder,
+                        "rf_splits_per_step": s_rf["rf_splits"] / kk,
+                        "redone_per_step": s_rf["mixed_cap_redone"] / kk,
+                        "fallbacks_per_step": s_rf["mixed_fallbacks"] / kk})
     sg.set_precision({"plain": "fp64", "mixed": "mixed", "mixed+learned": "mixed+learned"}[args.form],
-                     contractions=args.contractions)
+                     contractions=args.contractions,
+                     range_finder=args.range_finder and args.form == "mixed+learned",
+                     power_iters=args.rf_power)
     _lib.check(_lib.load().sm_ctx_set_rank_cap(_lib.context(), args.cap_margin, args.cap_extra))
 
     for _ in range(max(3, args.warmup)):
@@ -926,6 +952,8 @@ def main():
             if no_predictor:
                 line["mixed_without_predictor"] = no_predictor
                 line["predictor_gain"] = value / no_predictor["value"] if no_predictor["value"] else None
+            if rf_form:
+                line["learned_other_use"] = rf_form
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -199,6 +199,24 @@ int sm_gemm_f64tc(void* ctx, int dtype, int opA, int opB, int M, int N, int K,
  * SM_ERR_TIMEOUT).  seemps2_gb300.batch sets it on its worker contexts. */
 int sm_ctx_set_concurrent(void* ctx, int on);
 
+/* Learned form (SM_PRECISION_MIXED_LEARNED) with on != 0: the predicted kept
+ * rank r (or rank_hint in its place when > 0, no model needed) sizes a
+ * randomized range finder (Halko, Martinsson and Tropp, SIAM Rev. 53, 2011):
+ * k = r + oversample columns of W Omega, power_iters subspace iterations
+ * (3xTF32 products, shifted CholeskyQR between them), B^T = W^T Q.  The FP32
+ * cluster factorisation then works on B^T (rows of length k) instead of W;
+ * the FP64 refinement against the exact W, the exact discarded weight and the
+ * redo with the full QR when the subspace missed weight are those of the QR
+ * cap.  Real operands; on = 0 (default) caps the QR instead.  No reference
+ * counterpart. */
+int sm_ctx_set_range_finder(void* ctx, int on, int oversample, int power_iters, int rank_hint);
+/* The range finder alone: BH (l x k, row-major) = W^T Q for W = A^T (want_u)
+ * or A (real A, m x n, l = the length of W's rows), Q an orthonormal basis of
+ * the range of W Omega after power_iters subspace iterations; k <= min(m, n,
+ * 640).  No reference counterpart. */
+int sm_range_finder(void* ctx, const double* A, int m, int n, int want_u, int k, int power_iters,
+                    double* BH, void* stream);
+
 /* FP64 products of the mixed forms (state norm, refinement, final estimate,
  * FP64 contractions): 1 (default) on the tensor cores as sm_gemm_f64tc, 0 on
  * the FP64 SIMT kernel.  SM_PRECISION_FP64 always uses the SIMT kernel. */
@@ -490,6 +508,7 @@ typedef struct sm_stats {
                                   m x n split (m >= n, x4 complex) */
   double cluster_bytes;        /* algorithmic bytes of the cluster launches: the split matrix read
                                   once and the converged rows written */
+  int64_t rf_splits;           /* mixed splits that ran the randomized range finder */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

@@ -85,6 +85,7 @@ class sm_stats(C.Structure):
         ("cluster_flops", C.c_double),
         ("cluster_alg_flops", C.c_double),
         ("cluster_bytes", C.c_double),
+        ("rf_splits", C.c_int64),
     ]
 
 
@@ -115,6 +116,8 @@ SIGNATURES = {
                                 C.c_int, vp, C.c_int, vp, C.c_int, vp]),
     "sm_ctx_set_fp64_products": (C.c_int, [vp, C.c_int]),
     "sm_ctx_set_concurrent": (C.c_int, [vp, C.c_int]),
+    "sm_ctx_set_range_finder": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "sm_range_finder": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]),
     "sm_ctx_set_rank_cap": (C.c_int, [vp, C.c_double, C.c_int]),
     "sm_two_site_matvec": (C.c_int, [vp, C.c_int, ip, vp, vp, vp, vp, vp, C.c_int, vp]),
     "sm_two_site_prepare": (C.c_int, [vp, ip, vp, vp, C.c_int, vp]),
@@ -312,16 +315,23 @@ class SplitTrace:
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed+learned": 2}
 
 
-def set_precision(mode: str, device: int = 0, contractions: str = "fp64") -> None:
+def set_precision(mode: str, device: int = 0, contractions: str = "fp64",
+                  range_finder: bool = False, oversample: int = 10, power_iters: int = 0,
+                  rank_hint: int = 0) -> None:
     """Arithmetic of the SVD splits: "fp64" (default, reference ranks), "mixed"
     (FP32 cluster factorisation refined by FP64 GEMMs) or "mixed+learned" (as
-    "mixed", with the installed rank predictor capping the FP32 QR)."""
+    "mixed", with the installed rank predictor capping the FP32 QR, or, with
+    range_finder=True, sizing a randomized range finder of predicted rank +
+    oversample columns and power_iters subspace iterations; rank_hint > 0 stands
+    in for the prediction)."""
     if mode not in PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {mode!r}")
     if contractions not in ("fp64", "fp32"):
         raise ValueError("contractions must be 'fp64' or 'fp32'")
     check(load().sm_ctx_set_precision(context(device), PRECISIONS[mode]))
     check(load().sm_ctx_set_contraction_bits(context(device), 32 if contractions == "fp32" else 64))
+    check(load().sm_ctx_set_range_finder(context(device), int(bool(range_finder)), int(oversample),
+                                         int(power_iters), int(rank_hint)))
 
 
 def stats_reset(timing: bool = False, device: int = 0):

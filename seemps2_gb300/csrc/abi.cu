@@ -524,6 +524,42 @@ int sm_ctx_set_rank_cap(void* ctx, double margin, int extra) {
   return SM_OK;
 }
 
+int sm_range_finder(void* ctx, const double* A, int m, int n, int want_u, int k, int power_iters,
+                    double* BH, void* stream) {
+  SM_GUARD_CTX(ctx);
+  if (!A || !BH || m < 1 || n < 1 || power_iters < 0 || power_iters > 8) {
+    set_error("sm_range_finder: invalid argument");
+    return SM_ERR_VALUE;
+  }
+  Ctx& c = *as_ctx(ctx);
+  cudaStream_t s = as_stream(stream);
+  int* status;
+  SM_CHECK(c.scratch("rf.status", 1, &status));
+  SM_CHECK(range_finder_bh(c, s, A, m, n, want_u != 0, k, power_iters, BH, status));
+  int* h = reinterpret_cast<int*>(c.pinned);
+  SM_CUDA_CHECK(cudaMemcpyAsync(h, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SM_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (*h) {
+    set_error("sm_range_finder: Cholesky pivot not positive");
+    return SM_ERR_LINALG;
+  }
+  return SM_OK;
+}
+
+int sm_ctx_set_range_finder(void* ctx, int on, int oversample, int power_iters, int rank_hint) {
+  SM_GUARD_CTX(ctx);
+  if (oversample < 0 || power_iters < 0 || power_iters > 8 || rank_hint < 0) {
+    set_error("sm_ctx_set_range_finder: oversample >= 0, 0 <= power_iters <= 8, rank_hint >= 0");
+    return SM_ERR_VALUE;
+  }
+  Ctx* c = as_ctx(ctx);
+  c->range_finder = on != 0;
+  c->rf_oversample = oversample;
+  c->rf_power = power_iters;
+  c->rf_rank_hint = rank_hint;
+  return SM_OK;
+}
+
 int sm_ctx_set_concurrent(void* ctx, int on) {
   SM_GUARD_CTX(ctx);
   as_ctx(ctx)->concurrent = on != 0;

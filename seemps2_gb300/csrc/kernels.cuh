@@ -52,6 +52,13 @@ struct Ctx {
   // learned rank cap of the FP32 QR: ceil(cap_margin * predicted) + cap_extra rows
   double cap_margin = 1.15;
   int cap_extra = 10;
+  // learned form: the predicted rank (or rf_rank_hint > 0 in its place) sizes a
+  // randomized range finder of rank + rf_oversample columns and rf_power
+  // subspace iterations instead of capping the QR
+  bool range_finder = false;
+  int rf_oversample = 10;
+  int rf_power = 0;
+  int rf_rank_hint = 0;
   int split_site = -1, split_n = 0;
   int prev_rank = 0;
   std::vector<double> prev_s;
@@ -189,6 +196,13 @@ bool gemm_cplx_oz_eligible(int M, int N, int K);
 int gemm_cplx_3m(Ctx& ctx, cudaStream_t st, int opA, int opB, int M, int N, int K, cplx alpha,
                  const cplx* A, int lda, const cplx* B, int ldb, cplx beta, cplx* C, int ldc,
                  bool fp64_accurate);
+// --- rangefinder.cu -------------------------------------------------------------
+// BH (l x k) = W^T Q for an orthonormal basis Q of range(W Omega) after
+// power_iters subspace iterations (W = A^T if want_u, else A; real); *status
+// becomes 1 if a Cholesky pivot was not positive.  k <= range_finder_max_k().
+int range_finder_max_k();
+int range_finder_bh(Ctx& ctx, cudaStream_t st, const double* A, int m, int n, bool want_u, int k,
+                    int power_iters, double* BH, int* status);
 // --- dmrg.cu -----------------------------------------------------------------
 template <typename T>
 int two_site_matvec(Ctx& ctx, cudaStream_t st, int a, int c, int b, int p1, int p2, int e, int g,

@@ -1485,10 +1485,17 @@ double allowed_discard(const sm_strategy& st, double norm2, double s0, int k, in
 
 }  // namespace
 
+// rf_k > 0 (real operands): instead of factoring W, the cluster factors
+// BH = W^T Q (l x rf_k) of a randomized range finder (rangefinder.cu) sized by
+// the predicted rank; its rows (length rf_k) map back to W's right singular
+// vectors by one product with BH^T, and everything after (refinement against
+// the exact W, exact discarded weight, redo when the subspace missed weight the
+// rank needs) is shared with the QR path, the range finder playing the capped
+// QR's part (qr_cap = rf_k).
 template <typename T>
 int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
                     bool want_u, T* left, T* right, SplitResult* out, bool* done, int qr_cap,
-                    bool* missed_out) {
+                    bool* missed_out, int rf_k = 0) {
   *done = false;
   *missed_out = false;
   const int kw = want_u ? n : m;
@@ -1496,7 +1503,13 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   const int k = std::min(kw, l);
   if (k < kMixedMinRank || strat.method == SM_DO_NOT_TRUNCATE || strat.tolerance <= 0.0)
     return SM_OK;
-  if (!split_cluster_fits<T>(kw, l)) return SM_OK;
+  if constexpr (sizeof(T) != sizeof(double)) rf_k = 0;
+  if (rf_k > 0 && (rf_k >= k || rf_k > range_finder_max_k() || !split_cluster_fits<T>(l, rf_k)))
+    rf_k = 0;
+  // the matrix the cluster factors: W (kw x l), or BH (l x rf_k)
+  const int ckw = rf_k > 0 ? l : kw, cl = rf_k > 0 ? rf_k : l;
+  if (rf_k > 0) qr_cap = rf_k;
+  if (rf_k == 0 && !split_cluster_fits<T>(kw, l)) return SM_OK;
   // the exact-weight rank rule resolves discarded weights down to the FP64
   // rounding of |A|^2 - kept (~ k eps |A|^2): tighter relative tolerances
   // take the FP64 path (counted as a fallback)
@@ -1505,13 +1518,13 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     ctx.stats.mixed_fallbacks += 1;
     return SM_OK;
   }
-  const int kcap = k + 32;  // the Jacobi writes 32 blocks of ceil(rows / 32)
+  const int kcap = std::min(ckw, cl) + 32;  // the Jacobi writes 32 blocks of ceil(rows / 32)
   T *rows, *V0, *V1, *Cb, *Gb, *Mb, *Fb;
   double *nrm, *s_sorted, *errors, *info, *cn;
   int* perm;
   JacobiCtl* ctl;
   SplitResult* res;
-  SM_CHECK(ctx.scratch("mx.rows", (size_t)kcap * l, &rows));
+  SM_CHECK(ctx.scratch("mx.rows", (size_t)kcap * cl, &rows));
   SM_CHECK(ctx.scratch("mx.nrm", (size_t)kcap, &nrm));
   SM_CHECK(ctx.scratch("mx.s", (size_t)kcap, &s_sorted));
   SM_CHECK(ctx.scratch("mx.err", (size_t)kcap + 1, &errors));
@@ -1519,7 +1532,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(ctx.scratch("mx.info", 8, &info));
   SM_CHECK(ctx.scratch("mx.ctl", 1, &ctl));
   float* vbuf;
-  SM_CHECK(ctx.scratch("mx.vbuf", split_cluster_vbuf_floats(want_u ? n : m), &vbuf));
+  SM_CHECK(ctx.scratch("mx.vbuf", split_cluster_vbuf_floats(ckw), &vbuf));
   SM_CHECK(ctx.scratch("mx.res", 1, &res));
   // RRQR stop: drop at most 1% of what the tolerance allows (never more than
   // 1e-10 of |A|^2, which the power step then suppresses further)
@@ -1535,12 +1548,34 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // therefore runs the full QR.
   if (qr_cap >= std::min(m, n)) thr_rel = thr_abs = 0.0;
   SM_CUDA_CHECK(cudaMemsetAsync(ctl, 0, sizeof(JacobiCtl), st));
-  if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
-  // a predicted rank caps the rank-revealing QR (qr_cap rows of R)
+  // a predicted rank caps the rank-revealing QR (qr_cap rows of R), or sizes
+  // the range finder
   if (qr_cap > 0) ctx.stats.mixed_capped += 1;
-  SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
-                                info, qr_cap, vbuf));
-  if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+  T* BH = nullptr;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (rf_k > 0) {
+      int* rf_status;
+      double* a2;
+      SM_CHECK(ctx.scratch("rf.BH", (size_t)l * rf_k, &BH));
+      SM_CHECK(ctx.scratch("rf.status", 1, &rf_status));
+      SM_CHECK(ctx.scratch("rf.a2", 2, &a2));
+      ctx.stats.rf_splits += 1;
+      SM_CHECK(range_finder_bh(ctx, st, A, m, n, want_u, rf_k, ctx.rf_power, BH, rf_status));
+      if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+      // BH (l x rf_k) is the cluster's W; A's own |A|^2 replaces |BH|^2 below
+      SM_CHECK(split_cluster_f32<T>(st, BH, l, rf_k, false, thr_rel, thr_abs, 40, rows, nrm,
+                                    kcap, ctl, info, 0, vbuf));
+      if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+      SM_CHECK(vdot<T>(ctx, st, (size_t)m * n, A, A, a2));
+      SM_CUDA_CHECK(cudaMemcpyAsync(info, a2, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  if (rf_k == 0) {
+    if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
+    SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
+                                  info, qr_cap, vbuf));
+    if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
+  }
   struct Head {
     JacobiCtl c;
     double info[7];
@@ -1571,16 +1606,16 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   {  // algorithmic FP32 work of the launch (QR reflectors, then Jacobi pairs x sweeps)
     const int keff = hc.nact;
     double fl = 0.0;
-    for (int j = 0; j < keff; ++j) fl += 4.0 * (kw - j) * std::max(0, l - j - 1);
+    for (int j = 0; j < keff; ++j) fl += 4.0 * (ckw - j) * std::max(0, cl - j - 1);
     const double rows = 32.0 * ((keff + 31) / 32);  // the Jacobi's 32 blocks, zero rows included
-    fl += 12.0 * l * (rows * (rows - 1) / 2) * hc.sweeps;
+    fl += 12.0 * cl * (rows * (rows - 1) / 2) * hc.sweeps;
     const double cf = sizeof(T) == sizeof(double) ? 1.0 : 4.0;
     ctx.stats.cluster_flops += cf * fl;
     // the split's algorithmic SVD work, 4 m n^2 + 8 n^3 (m >= n), and its
     // algorithmic bytes: the matrix read once, the converged rows written
     const double mm = std::max(m, n), nn = std::min(m, n);
     ctx.stats.cluster_alg_flops += cf * (4.0 * mm * nn * nn + 8.0 * nn * nn * nn);
-    ctx.stats.cluster_bytes += (double)sizeof(T) * ((double)m * n + (double)keff * l);
+    ctx.stats.cluster_bytes += (double)sizeof(T) * ((double)ckw * cl + (double)keff * cl);
   }
   if (hc.status != 0 || (!exact_rule && h->info[3] < kMixedBlind * h->info[2])) {
     ctx.stats.mixed_fallbacks += 1;
@@ -1588,7 +1623,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     if (hc.status != 0) ctx.stats.mixed_fallback_unconverged += 1;
     return SM_OK;
   }
-  const int cnt = std::max(1, std::min(hc.nact, k));
+  const int cnt = std::max(1, std::min(hc.nact, std::min(ckw, cl)));
   ctx.stats.mixed_rows += cnt;
   SM_CHECK(ctx.scratch("mx.V0", (size_t)cnt * l, &V0));
   SM_CHECK(ctx.scratch("mx.V1", (size_t)cnt * l, &V1));
@@ -1597,11 +1632,22 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(ctx.scratch("mx.M", (size_t)cnt * cnt, &Mb));
   SM_CHECK(ctx.scratch("mx.F", (size_t)cnt * cnt, &Fb));
   SM_CHECK(ctx.scratch("mx.cn", (size_t)cnt, &cn));
-  // rows by decreasing norm (sorted above), normalised
-  k_gather_rows<T><<<grid_for((size_t)cnt * l), 256, 0, st>>>(rows, l, perm, s_sorted, cnt, V0);
-  note_launch();
-  SM_CUDA_CHECK(cudaGetLastError());
   const T one = S<T>::one(), zero = S<T>::zero();
+  if (rf_k == 0) {
+    // rows by decreasing norm (sorted above), normalised
+    k_gather_rows<T><<<grid_for((size_t)cnt * l), 256, 0, st>>>(rows, l, perm, s_sorted, cnt, V0);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+  } else {
+    // the rows of U_B^T (sorted, normalised), then W's right singular vectors
+    // U_B^T B = U_B^T BH^T (rows of norm sigma), normalised below
+    k_gather_rows<T><<<grid_for((size_t)cnt * rf_k), 256, 0, st>>>(rows, rf_k, perm, s_sorted, cnt,
+                                                                    V1);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, cnt, l, rf_k, one, V1, rf_k, BH, rf_k, zero, V0,
+                         l));
+  }
   // C = W V^H (kw x cnt)
   auto w_vh = [&](const T* V, T* C) -> int {
     if (want_u) return gemm_ctx<T>(ctx, st, SM_OP_T, SM_OP_C, n, cnt, m, one, A, n, V, m, zero, C, cnt);
@@ -1615,10 +1661,17 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     SM_CUDA_CHECK(cudaGetLastError());
     return SM_OK;
   };
+  if (rf_k > 0) SM_CHECK(normalise(V0));
   // 2. refinement (V0 holds the normalised FP32 rows)
   T* V = V0;
   T* Vn = V1;
-  for (int it = 0; it < kMixedRefine; ++it) {
+  // the range finder's rows come from the small side (U_B^T Q, length rf_k):
+  // mapping them to W's row space multiplies their FP32 error by the condition
+  // of the kept spectrum (1e-7 (s_max / s_i)^2 on a row of singular value s_i,
+  // against 1e-7 s_max / s_i for rows that the Jacobi forms in W's row space),
+  // which two more quadratically convergent steps take back to FP64 level
+  const int refine_steps = rf_k > 0 ? kMixedRefine + 2 : kMixedRefine;
+  for (int it = 0; it < refine_steps; ++it) {
     SM_CHECK(w_vh(V, Cb));
     SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
     SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, cnt, cnt, l, one, V, l, V, l, zero, Mb, cnt));
@@ -1727,18 +1780,22 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
   const bool xu = left_mode == OUT_U && right_mode == OUT_SVT;
   const bool xv = left_mode == OUT_US && right_mode == OUT_VT;
   if ((xu || xv) && ctx.precision != SM_PRECISION_FP64 && !s_out) {
-    int cap = 0;
-    if (ctx.precision == SM_PRECISION_MIXED_LEARNED && ctx.model.loaded &&
+    int cap = 0, rf_k = 0;
+    const bool hint = ctx.range_finder && ctx.rf_rank_hint > 0;
+    if (ctx.precision == SM_PRECISION_MIXED_LEARNED && (ctx.model.loaded || hint) &&
         std::min(m, n) >= kMixedMinRank && strat.method == SM_RELATIVE_NORM_SQUARED_ERROR &&
         strat.tolerance >= kMixedMinTol) {
-      int r = 0;
-      SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
+      int r = ctx.rf_rank_hint;
+      if (!hint) SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
       cap = std::min(std::min(m, n), (int)std::ceil(ctx.cap_margin * r) + ctx.cap_extra);
+      // the range finder at the predicted rank + oversampling (used when that
+      // is below min(m, n); otherwise the split keeps the QR path)
+      if (ctx.range_finder) rf_k = std::min(std::min(m, n), r + ctx.rf_oversample);
       ctx.stats.rank_predicted_sum += r;
     }
     bool done = false, missed = false;
     SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, cap,
-                                &missed));
+                                &missed, rf_k));
     if (done) return SM_OK;
     if (missed)  // predicted rank too small: the full QR
       SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done,

@@ -149,3 +149,100 @@ def test_mixed_learned_apply_matches_oracle(trained):
     assert stats["mixed_fallbacks"] <= 0.3 * stats["mixed_capped"], info
     fe = so.fidelity_error(mps_np(out), res.tensors)
     assert fe < 1e-10, fe
+
+
+def _workload_split(rng, m, n):
+    """A numerically rank-deficient m x n matrix with the spectrum of the n=30, chi=256
+    workload's splits: 256 values from 1 to 3e-3, two more near 2.5e-3, then zeros."""
+    s = np.concatenate([np.geomspace(1.0, 3e-3, 256), [2.5e-3, 2.4e-3]])
+    Qa, _ = np.linalg.qr(rng.normal(size=(m, len(s))))
+    Qb, _ = np.linalg.qr(rng.normal(size=(n, len(s))))
+    return (Qa * s) @ Qb.T
+
+
+@pytest.mark.parametrize("power_iters", [0, 1])
+def test_range_finder_captures_the_numerical_range(power_iters):
+    """sm_range_finder on a rank-258 512 x 480 matrix at k = 266: the 258 singular values of
+    BH = W^T Q above the rounding level equal W's within 1e-7 s_max without subspace
+    iterations (the Cholesky shift costs the sketch's worst-conditioned directions some
+    orthonormality) and within 1e-9 s_max with one; the 8 directions beyond the rank stay
+    below 1e-7 s_max; |BH|_F^2 = |W|_F^2 to 1e-8 relative.  The split refines its vectors
+    against the exact matrix, so the sketch needs only this much."""
+    import ctypes as C  # noqa: F401
+
+    rng = np.random.default_rng(21)
+    m, n, k = 512, 480, 266
+    A = _workload_split(rng, m, n)
+    Ad = torch.from_numpy(A).cuda()
+    for want_u in (0, 1):
+        W = A.T if want_u else A
+        BH = torch.empty((W.shape[1], k), dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().sm_range_finder(_lib.context(), _lib.ptr(Ad), m, n, want_u, k,
+                                               power_iters, _lib.ptr(BH), _lib.stream_handle()))
+        sb = np.linalg.svd(BH.cpu().numpy(), compute_uv=False)
+        sw = np.linalg.svd(W, compute_uv=False)[:k]
+        bar = 1e-7 if power_iters == 0 else 1e-9
+        assert np.max(np.abs(sb[:258] - sw[:258])) <= bar * sw[0], (power_iters, want_u)
+        assert np.max(sb[258:]) <= 1e-7 * sw[0], (power_iters, want_u, sb[258:])
+        assert abs(np.sum(sb**2) - np.sum(sw**2)) <= 1e-8 * np.sum(sw**2)
+
+
+@pytest.mark.parametrize("shape", [(512, 512), (768, 512), (512, 768)])
+def test_range_finder_split_matches_oracle(shape):
+    """Two-site splits of workload-shaped matrices through the learned form's range finder
+    (rank hint 256, k = 266): the kept rank, the discarded weight and the truncated product
+    agree with the oracle's (relative-norm tolerance 1e-12, max bond 256; the product within
+    1e-5 relative, i.e. fidelity 1e-10 as for the other mixed splits; sqrt(discarded weight)
+    within 1e-8); the split runs the
+    range finder and falls back to neither the full QR nor FP64."""
+    from seemps2_gb300 import core
+
+    rng = np.random.default_rng(sum(shape))
+    m, n = shape
+    AA = _workload_split(rng, m, n).reshape(m // 2, 2, 2, n // 2)
+    st = sg.Strategy(tolerance=1e-12, max_bond_dimension=256)
+    ost = so.Strategy(tolerance=1e-12, max_bond_dimension=256)
+    for gpu_fn, ora_fn in [(core._left_orth_2site, so.left_orth_2site),
+                           (core._right_orth_2site, so.right_orth_2site)]:
+        sg.set_precision("mixed+learned", range_finder=True, rank_hint=256)
+        _lib.stats_reset()
+        try:
+            L, R, err = gpu_fn(AA, st)
+            stats = _lib.stats_read()
+        finally:
+            sg.set_precision("fp64")
+        Lo, Ro, erro = ora_fn(AA, ost)
+        info = {k: stats[k] for k in ("rf_splits", "mixed_fallbacks", "mixed_cap_redone",
+                                      "mixed_fallback_cut", "mixed_fallback_over")}
+        assert stats["rf_splits"] == 1 and stats["mixed_fallbacks"] == 0, info
+        assert stats["mixed_cap_redone"] == 0, info
+        D = L.shape[-1]
+        assert D == Lo.shape[-1]
+        rec = L.cpu().numpy().reshape(-1, D) @ R.cpu().numpy().reshape(D, -1)
+        reco = Lo.reshape(-1, D) @ Ro.reshape(D, -1)
+        assert np.linalg.norm(rec - reco) <= 1e-5 * np.linalg.norm(reco)
+        assert abs(err - erro) <= 1e-8 * max(1.0, erro)
+
+
+def test_range_finder_apply_matches_oracle(trained):
+    """The learned form with the range finder sized by the trained predictor: MPO.apply of
+    the Laplacian within 1e-10 fidelity of the FP64 oracle; splits whose subspace missed
+    weight are redone with the full QR."""
+    model, *_ = trained
+    model.install()
+    rng = np.random.default_rng(7)
+    n, chi = 14, 64
+    mps, mpo = learned.laplacian_case(n, chi, rng)
+    kw = dict(tolerance=1e-12, max_bond_dimension=chi, max_sweeps=2, simplification_tolerance=0.0)
+    st = sg.DEFAULT_STRATEGY.replace(**kw)
+    sg.set_precision("mixed+learned", range_finder=True)
+    _lib.stats_reset()
+    try:
+        out = sg.MPO(mpo, st).apply(sg.MPS(mps), strategy=st)
+        stats = _lib.stats_read()
+    finally:
+        sg.set_precision("fp64")
+    res = so.mpo_apply(mpo, mps, so.DEFAULT_STRATEGY.replace(**kw))
+    assert stats["rf_splits"] > 5, stats
+    fe = so.fidelity_error(mps_np(out), res.tensors)
+    assert fe < 1e-10, fe
