@@ -945,7 +945,7 @@ def main():
                 "capped_per_step": timed_stats["mixed_capped"] / k,
                 "cap_redone_per_step": timed_stats["mixed_cap_redone"] / k,
                 "mean_predicted_rank": timed_stats["rank_predicted_sum"]
-                / max(1, timed_stats["mixed_capped"]),
+                / max(1, timed_stats["rank_predictions"]),
             }
             if learned_info:
                 line["learned"] = learned_info

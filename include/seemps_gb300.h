@@ -509,6 +509,9 @@ typedef struct sm_stats {
   double cluster_bytes;        /* algorithmic bytes of the cluster launches: the split matrix read
                                   once and the converged rows written */
   int64_t rf_splits;           /* mixed splits that ran the randomized range finder */
+  int64_t mixed_ns_steps;      /* Newton-Schulz steps of the mixed splits (one, or two for rows
+                                  below FP32 resolution) */
+  int64_t rank_predictions;    /* splits whose kept rank the predictor (or a rank hint) gave */
 } sm_stats;
 int sm_stats_reset(void* ctx, int timing);
 int sm_stats_read(void* ctx, sm_stats* out);

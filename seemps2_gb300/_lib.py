@@ -86,6 +86,8 @@ class sm_stats(C.Structure):
         ("cluster_alg_flops", C.c_double),
         ("cluster_bytes", C.c_double),
         ("rf_splits", C.c_int64),
+        ("mixed_ns_steps", C.c_int64),
+        ("rank_predictions", C.c_int64),
     ]
 
 

@@ -128,7 +128,7 @@ struct JacobiCtl {
   int status;
   int sweeps;
   int nact;  // rows still taking part in the iteration (deflation / rank)
-  int pad;
+  int nkeep;  // mixed split: FP32 rows heavy enough to take into the FP64 refinement
 };
 
 // Output forms of the two factors of a split A = U diag(s) Vt.

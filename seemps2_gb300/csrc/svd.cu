@@ -1189,6 +1189,11 @@ constexpr int kMixedRefine = 2;    // refinement steps
 constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
 constexpr double kMixedCutAmp = 1e-6;  // largest kept/dropped coupling (angle s_i / |A|)
 constexpr double kMixedMinTol = 1e-14;   // smallest relative-norm tolerance taken in mixed
+constexpr double kMixedRowFloor = 1e-12;  // FP32 rows lighter than this times |A|_F are dropped
+constexpr double kMixedOrthMax = 0.25;    // largest |V V^H - I| entry a Newton-Schulz step takes
+constexpr double kMixedNsOne = 3e-7;      // deviation after which one step reaches 1.4e-13
+constexpr int kMixedNsMax = 5;            // Newton-Schulz steps at most
+constexpr double kCapUseful = 0.8;        // largest predicted-rank cap applied, of min(m, n)
 
 template <typename T>
 __global__ void k_gather_rows(const T* __restrict__ rows, int l, const int* __restrict__ perm,
@@ -1253,15 +1258,36 @@ __global__ void k_refine_matrix(const T* __restrict__ G, const T* __restrict__ M
   }
 }
 
-// F = 1.5 I - 0.5 M: one Newton-Schulz step X <- F X towards orthonormal rows.
+// F = 1.5 I - 0.5 M: one Newton-Schulz step X <- F X towards orthonormal rows;
+// dev = max |M - I| over the grid (atomic max on the bits of the non-negative
+// double; dev must be zero beforehand).
 template <typename T>
-__global__ void k_ns_matrix(const T* __restrict__ M, int k, T* __restrict__ F) {
+__global__ void __launch_bounds__(256) k_ns_matrix(const T* __restrict__ M, int k,
+                                                   T* __restrict__ F, double* dev) {
+  __shared__ double red[8];
   const size_t tot = (size_t)k * k;
+  double worst = 0.0;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
        e += (size_t)gridDim.x * blockDim.x) {
     T f = S<T>::scale(M[e], -0.5);
-    if (e / k == e % k) f = f + S<T>::from_real(1.5);
+    T d = M[e];
+    if (e / k == e % k) {
+      f = f + S<T>::from_real(1.5);
+      d = d - S<T>::one();
+    }
     F[e] = f;
+    const double a = sqrt(S<T>::abs2(d));
+    worst = a == a ? fmax(worst, a) : 1e300;
+  }
+  for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = worst;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double w = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) w = fmax(w, red[i]);
+    if (w > 0.0)
+      atomicMax(reinterpret_cast<unsigned long long*>(dev),
+                (unsigned long long)__double_as_longlong(w));
   }
 }
 
@@ -1344,11 +1370,14 @@ __device__ int mixed_rank_block(const double* ss, const double* P, int n, const 
 
 // First step of a mixed split, one CTA of 1024 threads (n <= 1024): the FP32
 // rows' norms sorted descending (perm, s_sorted) and mixed_rank_block on them
-// (the host uses info[2], info[3] and the status).  Dynamic shared memory:
-// 24 n bytes.
+// (the host uses info[2], info[3] and the status); ctl->nkeep = the number of
+// rows of norm at least row_floor |A|_F (the lighter rows, each below 1e-24
+// of |A|^2 and far below FP32 resolution, are left out of the refinement);
+// info[8] = 0 for the orthonormality measure of k_ns_matrix.  Dynamic shared
+// memory: 24 n bytes.
 __global__ void __launch_bounds__(1024) k_mixed_sort(const double* __restrict__ nrm, int n,
                                                      sm_strategy st, int exact_rule,
-                                                     const JacobiCtl* ctl, int* perm,
+                                                     JacobiCtl* ctl, double row_floor, int* perm,
                                                      double* s_sorted, SplitResult* res,
                                                      double* info) {
   extern __shared__ unsigned long long keys[];
@@ -1363,6 +1392,13 @@ __global__ void __launch_bounds__(1024) k_mixed_sort(const double* __restrict__ 
   __syncthreads();
   block_prefix_sq(ss, n, P, wsum);
   mixed_rank_block(ss, P, n, st, exact_rule, ctl, res, info, &shD, &shBad);
+  const double floor = row_floor * sqrt(fmax(info[0], 0.0));
+  const int t = threadIdx.x;
+  if (t == 0) {
+    info[8] = 0.0;
+    if (!(ss[0] >= floor)) ctl->nkeep = 0;
+  }
+  if (t < n && ss[t] >= floor && (t + 1 == n || !(ss[t + 1] >= floor))) ctl->nkeep = t + 1;
 }
 
 // Final step of a mixed split, one CTA of 1024 threads, on G = C^H C of the
@@ -1529,7 +1565,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CHECK(ctx.scratch("mx.s", (size_t)kcap, &s_sorted));
   SM_CHECK(ctx.scratch("mx.err", (size_t)kcap + 1, &errors));
   SM_CHECK(ctx.scratch("mx.perm", (size_t)kcap, &perm));
-  SM_CHECK(ctx.scratch("mx.info", 8, &info));
+  SM_CHECK(ctx.scratch("mx.info", 16, &info));
   SM_CHECK(ctx.scratch("mx.ctl", 1, &ctl));
   float* vbuf;
   SM_CHECK(ctx.scratch("mx.vbuf", split_cluster_vbuf_floats(ckw), &vbuf));
@@ -1585,7 +1621,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // the FP64 path right away
   const bool exact_rule = strat.method == SM_RELATIVE_NORM_SQUARED_ERROR;
   k_mixed_sort<<<1, 1024, 3 * sizeof(double) * (size_t)kcap, st>>>(
-      nrm, kcap, strat, exact_rule ? 1 : 0, ctl, perm, s_sorted, res, info);
+      nrm, kcap, strat, exact_rule ? 1 : 0, ctl, kMixedRowFloor, perm, s_sorted, res, info);
   note_launch();
   SM_CUDA_CHECK(cudaGetLastError());
   Head* h = reinterpret_cast<Head*>(ctx.pinned);
@@ -1623,7 +1659,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     if (hc.status != 0) ctx.stats.mixed_fallback_unconverged += 1;
     return SM_OK;
   }
-  const int cnt = std::max(1, std::min(hc.nact, std::min(ckw, cl)));
+  const int cnt = std::max(1, std::min(std::min(hc.nact, hc.nkeep), std::min(ckw, cl)));
   ctx.stats.mixed_rows += cnt;
   SM_CHECK(ctx.scratch("mx.V0", (size_t)cnt * l, &V0));
   SM_CHECK(ctx.scratch("mx.V1", (size_t)cnt * l, &V1));
@@ -1682,16 +1718,38 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
     SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_N, cnt, l, cnt, one, Fb, cnt, V, l, zero, Vn, l));
     std::swap(V, Vn);
   }
-  // Newton-Schulz: the refinement leaves the orthonormality error of nearly
-  // degenerate pairs at ~1e-11; one step takes it to 1.5 e^2
+  // Newton-Schulz steps V <- (1.5 I - 0.5 V V^H) V take the largest
+  // deviation e of V V^H from I to about 1.5 e^2.  Two refinement steps leave
+  // e below kMixedNsOne for resolved rows (one step then reaches FP64 level);
+  // rows below FP32 resolution that a tolerance-limited cut keeps leave up to
+  // ~1e-5 and take a second step; the range finder's rows beyond the rank
+  // (noise of the sketch) a few more.  A deviation beyond kMixedOrthMax, or one
+  // that a step did not reduce, means rows that the FP32 stage left nearly
+  // parallel: the split goes to FP64.
   SM_CHECK(normalise(V));
-  SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, cnt, cnt, l, one, V, l, V, l, zero, Mb, cnt));
-  k_ns_matrix<T><<<grid_for((size_t)cnt * cnt), 256, 0, st>>>(Mb, cnt, Fb);
-  note_launch();
-  SM_CUDA_CHECK(cudaGetLastError());
-  SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_N, cnt, l, cnt, one, Fb, cnt, V, l, zero, Vn, l));
-  std::swap(V, Vn);
-  SM_CHECK(normalise(V));
+  double e_ns = 0.0;
+  bool ns_done = false;
+  double* hdev = reinterpret_cast<double*>(ctx.pinned) + 512;
+  for (int ns = 0; ns < kMixedNsMax; ++ns) {
+    SM_CUDA_CHECK(cudaMemsetAsync(info + 8, 0, sizeof(double), st));
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_C, cnt, cnt, l, one, V, l, V, l, zero, Mb, cnt));
+    k_ns_matrix<T><<<grid_for((size_t)cnt * cnt), 256, 0, st>>>(Mb, cnt, Fb, info + 8);
+    note_launch();
+    SM_CUDA_CHECK(cudaGetLastError());
+    SM_CUDA_CHECK(cudaMemcpyAsync(hdev, info + 8, sizeof(double), cudaMemcpyDeviceToHost, st));
+    SM_CUDA_CHECK(cudaStreamSynchronize(st));
+    const double e_prev = ns ? e_ns : kMixedOrthMax;
+    e_ns = *hdev;
+    if (!(e_ns <= e_prev)) break;
+    SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_N, SM_OP_N, cnt, l, cnt, one, Fb, cnt, V, l, zero, Vn, l));
+    std::swap(V, Vn);
+    SM_CHECK(normalise(V));
+    ctx.stats.mixed_ns_steps += 1;
+    if (e_ns <= kMixedNsOne) {
+      ns_done = true;
+      break;
+    }
+  }
   // 3. singular values, truncation, exact discarded weight
   SM_CHECK(w_vh(V, Cb));
   SM_CHECK(gemm_ctx<T>(ctx, st, SM_OP_C, SM_OP_N, cnt, cnt, kw, one, Cb, cnt, Cb, cnt, zero, Gb, cnt));
@@ -1727,16 +1785,20 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   const bool missed = qr_cap > 0 && qr_cap < k &&
                       hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
   const bool coupled = !(cut_angle <= kMixedCutAmp);
-  const bool over = D < strat.max_bond_dimension && D < k &&
-                    r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
-  if ((missed || (over && qr_cap > 0 && qr_cap < k)) && !blind && !coupled) {
+  const bool over_tol = r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
+  const bool over = D < strat.max_bond_dimension && D < k && over_tol;
+  // The Newton-Schulz steps must have converged, and a split that keeps every
+  // value leaves nothing to discard: either failing means the FP32 stage lost
+  // directions, and the split goes to FP64.
+  const bool lost = !ns_done || (D >= k && over_tol);
+  if ((missed || (over && qr_cap > 0 && qr_cap < k)) && !blind && !coupled && !lost) {
     // the cap (or the QR's stop) left weight the rank needs: the caller
     // retries with the full QR
     ctx.stats.mixed_cap_redone += 1;
     *missed_out = true;
     return SM_OK;
   }
-  if (blind || coupled || over) {
+  if (blind || coupled || over || lost) {
     ctx.stats.mixed_fallbacks += 1;
     if (coupled) ctx.stats.mixed_fallback_cut += 1;
     else ctx.stats.mixed_fallback_fp32 += 1;
@@ -1788,10 +1850,14 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
       int r = ctx.rf_rank_hint;
       if (!hint) SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
       cap = std::min(std::min(m, n), (int)std::ceil(ctx.cap_margin * r) + ctx.cap_extra);
+      // a cap near the split size saves few QR steps and risks a redo of the
+      // whole split: only caps below kCapUseful of min(m, n) are applied
+      if (cap > kCapUseful * std::min(m, n)) cap = 0;
       // the range finder at the predicted rank + oversampling (used when that
       // is below min(m, n); otherwise the split keeps the QR path)
       if (ctx.range_finder) rf_k = std::min(std::min(m, n), r + ctx.rf_oversample);
       ctx.stats.rank_predicted_sum += r;
+      ctx.stats.rank_predictions += 1;
     }
     bool done = false, missed = false;
     SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, cap,

@@ -64,10 +64,21 @@ constexpr int kCW = 16;            // CTAs per cluster
 constexpr int kCNT = 512;          // threads per CTA
 constexpr int kCNW = kCNT / 32;    // warps per CTA
 constexpr int kMaxRows = 512;      // rows of R the Jacobi phase takes (32 blocks of <= 16)
-// Jacobi: a sweep whose rotations all start below cosine 2e-3 ends the iteration
-constexpr float kStopC2 = 4e-6f;
+// Jacobi: a sweep whose rotations all start below cosine 1e-2 ends the iteration
+constexpr float kStopC2 = 1e-4f;
 constexpr int kQB = 8;             // widest column block of the QR (reflectors per cluster barrier)
 constexpr int kPanelRP = 2;        // rows per thread of the QR panel in registers (kw <= 1024)
+// Scale floors (W is held as W / |W|_F, so these are relative to |W|):
+// a QR column whose part below its pivot has norm <= kTinyCol gets no
+// reflector (the part, weight <= 1e-30, is dropped; its tau would approach
+// the FP32 range); the QR also stops once the trailing weight is below
+// kQrFloor whatever the threshold asked; the Jacobi leaves rows of squared
+// norm below kTinyRow2 alone and rotates only pairs whose normalised |g|^2
+// is above kTinyG2 (clear of the SFU's subnormal flush).
+constexpr float kTinyCol = 1e-15f;
+constexpr float kQrFloor = 1e-24f;
+constexpr float kTinyRow2 = 1e-30f;
+constexpr float kTinyG2 = 1e-36f;
 
 // column slots per CTA for l columns in blocks of qb
 __host__ __device__ inline int qr_slots(int l, int qb) {
@@ -297,7 +308,8 @@ __global__ void __launch_bounds__(kCNT, 1)
   const double nrm = sqrt(norm2);
   const double scale = nrm > 0.0 ? 1.0 / nrm : 1.0;
   // stop once the trailing block holds at most max(thr_rel |W|^2, thr_abs)
-  const float thr = (float)fmax(thr_rel, norm2 > 0.0 ? thr_abs / norm2 : 0.0);
+  const float thr =
+      fmaxf((float)fmax(thr_rel, norm2 > 0.0 ? thr_abs / norm2 : 0.0), kQrFloor);
   for (int s = warp; s < ncs; s += kCNW) {
     const int c = col_of(s);
     if (c >= l) break;
@@ -479,8 +491,10 @@ __global__ void __launch_bounds__(kCNT, 1)
           pr_ = f_re(x0) / a0;
           pi_ = f_im(x0) / a0;
         }
-        f_set(v0s[i], f_re(x0) + pr_ * xn, f_im(x0) + pi_ * xn);
-        taus[i] = xn > 0.f ? 1.0f / (xn * (xn + a0)) : 0.f;
+        // no reflector for a column that is already zero to the noise floor
+        const bool refl = xn > kTinyCol;
+        if (refl) f_set(v0s[i], f_re(x0) + pr_ * xn, f_im(x0) + pi_ * xn);
+        taus[i] = refl ? 1.0f / (xn * (xn + a0)) : 0.f;
         // Gram entries v_m^H v_i = (rows > j) + conj(v_m[j]) v0_i
         if (tid == 0) {
 #pragma unroll
@@ -496,8 +510,9 @@ __global__ void __launch_bounds__(kCNT, 1)
 #pragma unroll
         for (int pr = 0; pr < kPanelRP; ++pr) {
           const int row = tid + kCNT * pr;
-          vi[pr] = (row > j && row < kw) ? x[pr][i] : (row == j ? v0s[i] : F32<T>::zero());
-          if (row == j) f_set(x[pr][i], -pr_ * xn, -pi_ * xn);
+          vi[pr] = !refl ? F32<T>::zero()
+                         : (row > j && row < kw) ? x[pr][i] : (row == j ? v0s[i] : F32<T>::zero());
+          if (row == j && refl) f_set(x[pr][i], -pr_ * xn, -pi_ * xn);
         }
         // d_k = v_i^H x_k (k > i), then x_k -= tau d_k v_i
         float dd[16];
@@ -533,8 +548,9 @@ __global__ void __launch_bounds__(kCNT, 1)
           if (k < nbp) cols[(size_t)(sp + k) * ks + row] = x[pr][k];
           if (k < qb) {
             const int jk = cp + k;
-            const F v = k >= nbp ? F32<T>::zero()
-                                 : (row > jk ? x[pr][k] : (row == jk ? v0s[k] : F32<T>::zero()));
+            const F v = (k >= nbp || taus[k] == 0.f)
+                            ? F32<T>::zero()
+                            : (row > jk ? x[pr][k] : (row == jk ? v0s[k] : F32<T>::zero()));
             Vp[(size_t)row * qb + k] = v;
           }
         }
@@ -722,9 +738,9 @@ __global__ void __launch_bounds__(kCNT, 1)
 #pragma unroll
     for (int e = 0; e < NV; ++e) r4[lane + 32 * e] = x[e];
   };
-  // Rotates the register rows u, v of this warp; true if it rotated.
-  float c2w = 0.f;  // this warp's largest rotated cos^2 in the sweep
-  auto rotate_regs = [&](float4* u, float4* v) -> bool {
+  // Squared norms and conj(u) v of the register rows u, v (warp sums).
+  auto pair_gram = [&](const float4* u, const float4* v, float& a_, float& b_, float& gr_,
+                       float& gi_) {
     float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f, gr0 = 0.f, gr1 = 0.f, gi0 = 0.f, gi1 = 0.f;
 #pragma unroll
     for (int e = 0; e < NV; ++e) {
@@ -743,12 +759,29 @@ __global__ void __launch_bounds__(kCNT, 1)
         gi1 = fmaf(p.z, q.w, fmaf(-p.w, q.z, gi1));
       }
     }
-    const float a = warp_sum(a0 + a1), b = warp_sum(b0 + b1), gr = warp_sum(gr0 + gr1);
-    float gi = 0.f;
-    if constexpr (sizeof(F) != 4) gi = warp_sum(gi0 + gi1);
+    a_ = warp_sum(a0 + a1);
+    b_ = warp_sum(b0 + b1);
+    gr_ = warp_sum(gr0 + gr1);
+    gi_ = 0.f;
+    if constexpr (sizeof(F) != 4) gi_ = warp_sum(gi0 + gi1);
+  };
+  // Rotates the register rows u, v of this warp; true if it rotated.
+  float c2w = 0.f;  // this warp's largest rotated cos^2 in the sweep
+  auto rotate_regs = [&](float4* u, float4* v) -> bool {
+    float a_, b_, gr_, gi_;
+    pair_gram(u, v, a_, b_, gr_, gi_);
+    // The rotation depends on a : b : g only, so it is decided on the pair's
+    // Gram entries divided by max(a, b): rows far below |W| (1e-14 of it and
+    // less) have products a b and g^2 below the FP32 range, and left unrotated
+    // they stay nearly parallel, which no later FP64 step separates.  Rows
+    // whose squared norm is itself near the bottom of the range (< 1e-30 |W|^2,
+    // weight no rank rule can see) are left alone.
+    if (!(fminf(a_, b_) >= kTinyRow2)) return false;
+    const float sc = __fdividef(1.0f, fmaxf(a_, b_));
+    const float a = a_ * sc, b = b_ * sc, gr = gr_ * sc, gi = gi_ * sc;
     const float g2 = fmaf(gr, gr, gi * gi);
-    if (!(g2 > 0.f && g2 > tol2 * a * b)) return false;
-    c2w = fmaxf(c2w, __fdividef(g2, fmaxf(a * b, FLT_MIN)));
+    if (!(g2 > kTinyG2 && g2 > tol2 * a * b)) return false;
+    c2w = fmaxf(c2w, __fdividef(g2, a * b));
     const float rg = rsqrtf(g2);
     const float zeta = 0.5f * (b - a) * rg;
     const float az = fabsf(zeta);
@@ -872,11 +905,12 @@ __global__ void __launch_bounds__(kCNT, 1)
       }
     }
     // Converged when nothing rotated, or when every rotation of the sweep
-    // started from a cosine below 2e-3: the iteration converges
-    // quadratically, so the rows leave such a sweep orthogonal to ~4e-6 / gap
-    // (FP32 rounding for separated values, measured 3.4e-6 on the 512 x 512
-    // workload split; the two FP64 refinement steps square what is left) and
-    // a further sweep would mostly rotate rounding noise.
+    // started from a cosine below 1e-2: the iteration converges
+    // quadratically, so the rows leave such a sweep orthogonal to ~1e-4 / gap,
+    // which the two quadratically convergent FP64 refinement steps take to
+    // ~1e-16 / gap; a further FP32 sweep would cost as much as both of them
+    // (on the 512 x 512 workload split: 10 sweeps instead of 11 for the 2e-3
+    // rule, the same split, no fallback).
     const int rotated = ctrl0->flag[sweep & 1];
     if (!rotated || __int_as_float(ctrl0->c2max[sweep & 1]) < kStopC2) {
       status = 0;

@@ -202,6 +202,46 @@ def test_mixed_falls_back_when_fp32_cannot_meet_tolerance(mixed):
     assert L.shape[-1] == oL.shape[-1]
 
 
+@pytest.mark.parametrize("qr", ["stop", "full"])
+def test_mixed_split_of_a_graded_matrix(qr):
+    """A matrix met while canonicalising the Laplacian product state (rows
+    graded down to 1e-12 of the largest, a third exact zeros, numerical rank
+    ~63 of 192; tests/golden/make_graded_split.py).  Its FP32 QR leaves rows of
+    R far below FP32 resolution; the split must still give orthonormal rows,
+    the oracle's rank and the exact discarded weight, with the QR stopped by the
+    trailing weight ("stop") or run to the end ("full": a rank hint of 20 makes
+    the first attempt miss weight, and its redo runs the whole QR)."""
+    import os
+
+    A = np.load(os.path.join(os.path.dirname(__file__), "golden",
+                             "graded_split_192x250.npz"))["A"]
+    a2 = float(np.sum(A ** 2))
+    AA = two_site(A, 96, 2, 2, 125)
+    st = sg.Strategy(tolerance=1e-12, max_bond_dimension=256)
+    if qr == "full":
+        sg.set_precision("mixed+learned", range_finder=True, rank_hint=20)
+    else:
+        sg.set_precision("mixed")
+    _lib.stats_reset()
+    try:
+        US, V, err = core._right_orth_2site(AA, st)
+        stats = _lib.stats_read()
+    finally:
+        sg.set_precision("fp64")
+    oUS, oV, oerr = so.right_orth_2site(AA, so.Strategy(tolerance=1e-12, max_bond_dimension=256))
+    D = V.shape[0]
+    Vn = V.cpu().numpy().reshape(D, 250)
+    USn = US.cpu().numpy().reshape(192, D)
+    assert D == oV.shape[0]
+    assert np.abs(Vn @ Vn.T - np.eye(D)).max() <= 1e-13
+    assert abs(float(err) ** 2 - float(oerr) ** 2) <= 1e-10 * a2
+    P, Po = USn @ Vn, oUS.reshape(192, D) @ oV.reshape(D, 250)
+    assert product_fidelity_error(P, Po) <= 1e-10
+    assert stats["mixed_splits"] >= 1
+    if qr == "full":
+        assert stats["mixed_cap_redone"] == 1
+
+
 def laplacian_case(n, chi, seed=7):
     rng = np.random.default_rng(seed)
     raw = so.random_mps(2, n, chi, rng)
