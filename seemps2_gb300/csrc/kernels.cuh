@@ -272,6 +272,10 @@ int rank_predict(Ctx& ctx, cudaStream_t st, int k, const sm_strategy& strat, int
 
 // --- svd_mixed.cu ------------------------------------------------------------
 // Whether the 16-CTA cluster factorisation holds W (kw x l) on this GPU.
+// Splits with min(m, n) below this stay on the FP64 path in the mixed forms.
+constexpr int kMixedMinRank = 24;
+template <typename T>
+bool split_cluster_size_ok(int kw, int l);
 template <typename T>
 bool split_cluster_fits(int kw, int l);
 // FP32 rank-revealing QR + one-sided Jacobi of W = (want_u ? A^T : A) in one

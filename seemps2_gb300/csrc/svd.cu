@@ -1184,7 +1184,6 @@ int svd_split_xfree(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int kMixedMinRank = 24;  // smaller splits stay on the FP64 path
 constexpr int kMixedRefine = 2;    // refinement steps
 constexpr double kMixedBlind = 1e-4;  // smallest kept s / s_max the FP32 stage resolves
 constexpr double kMixedCutAmp = 1e-6;  // largest kept/dropped coupling (angle s_i / |A|)

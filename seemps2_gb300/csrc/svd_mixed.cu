@@ -185,7 +185,7 @@ struct CtrlS {
   int flag[2];                 // CTA 0: a rotation happened in the sweep of this parity
   int c2max[2];                // CTA 0: largest rotated cos^2 of that sweep (float bits)
   float2 gram[kQB][kQB];       // panel reflector Gram matrix v_i^H v_k (i < k; re, im)
-  float2 prow[kQB];            // the panel's pivot row (re, im), while it is factored
+  float2 prow[2][kQB];         // the panel's pivot row (re, im), by reflector parity
   float rsq[kQB][kQB];         // |R|^2 of the rows just below the panel's first row
   float pred[kCNW][16];        // CTA-sum partials
   float pfin[16];
@@ -448,21 +448,27 @@ __global__ void __launch_bounds__(kCNT, 1)
       v0s[i] = F32<T>::zero();
       taus[i] = 0.f;
     }
-    // reflectors one by one (v_m on a row below its pivot is the column's
-    // stored value)
+    // Reflectors one by one (v_m on a row below its pivot is the column's
+    // stored value), one CTA-wide sum each: with the pivot row's values
+    // broadcast first, the column norm, the Gram entries v_m^H v_i (m < i) and
+    // the products d_k = v_i^H x_k (k > i) all come from sums over the rows
+    // below the pivot, v_i being x_i there (d_k adds conj(v0_i) x_k[j] after
+    // the sum).  The pivot values alternate between two buffers, so a step's
+    // writes never meet the previous step's reads (one barrier apart).
 #pragma unroll
     for (int i = 0; i < kQB; ++i) {
       if (i < nbp) {
         const int j = cp + i;
-        // the pivot row's values: x_i[j] and v_m[j] = x_m[j] (m < i)
+        float2* prw = ctrl->prow[i & 1];
 #pragma unroll
         for (int pr = 0; pr < kPanelRP; ++pr)
           if (tid + kCNT * pr == j) {
 #pragma unroll
-            for (int m = 0; m <= i; ++m)
-              ctrl->prow[m] = make_float2(f_re(x[pr][m]), f_im(x[pr][m]));
+            for (int m = 0; m < kQB; ++m)
+              if (m < nbp) prw[m] = make_float2(f_re(x[pr][m]), f_im(x[pr][m]));
           }
-        // |x_i|^2 over rows >= j; sum over rows > j of conj(v_m) x_i (m < i)
+        // red[0] = |x_i|^2 over rows >= j; over rows > j, slots 1 + 2 s, 2 + 2 s:
+        // conj(x_m) x_i for m < i (s = m), conj(x_i) x_k for k > i (s = k - 1)
         float red[16];
 #pragma unroll
         for (int a = 0; a < 16; ++a) red[a] = 0.f;
@@ -472,16 +478,23 @@ __global__ void __launch_bounds__(kCNT, 1)
           if (row >= j && row < kw) red[0] += f_abs2(x[pr][i]);
           if (row > j && row < kw) {
 #pragma unroll
-            for (int m = 0; m < i; ++m) {
-              float gr = 0.f, gi = 0.f;
-              f_dotc(x[pr][m], x[pr][i], gr, gi);
-              red[1 + 2 * m] += gr;
-              red[2 + 2 * m] += gi;
+            for (int m = 0; m < kQB; ++m) {
+              if (m < i) {
+                float gr = 0.f, gi = 0.f;
+                f_dotc(x[pr][m], x[pr][i], gr, gi);
+                red[1 + 2 * m] += gr;
+                red[2 + 2 * m] += gi;
+              } else if (m > i && m < nbp) {
+                float gr = 0.f, gi = 0.f;
+                f_dotc(x[pr][i], x[pr][m], gr, gi);
+                red[2 * m - 1] += gr;
+                red[2 * m] += gi;
+              }
             }
           }
         }
-        cta_sum(ctrl, red, 1 + 2 * i);
-        const float2 xp = ctrl->prow[i];
+        cta_sum(ctrl, red, 2 * nbp - 1);
+        const float2 xp = prw[i];
         F x0;
         f_set(x0, xp.x, xp.y);
         const float xn = sqrtf(red[0]);
@@ -495,13 +508,14 @@ __global__ void __launch_bounds__(kCNT, 1)
         const bool refl = xn > kTinyCol;
         if (refl) f_set(v0s[i], f_re(x0) + pr_ * xn, f_im(x0) + pi_ * xn);
         taus[i] = refl ? 1.0f / (xn * (xn + a0)) : 0.f;
+        const float v0r = f_re(v0s[i]), v0i = f_im(v0s[i]);
         // Gram entries v_m^H v_i = (rows > j) + conj(v_m[j]) v0_i
         if (tid == 0) {
 #pragma unroll
           for (int m = 0; m < i; ++m) {
-            const float2 vm = ctrl->prow[m];
-            const float gr = red[1 + 2 * m] + vm.x * f_re(v0s[i]) + vm.y * f_im(v0s[i]);
-            const float gi = red[2 + 2 * m] + vm.x * f_im(v0s[i]) - vm.y * f_re(v0s[i]);
+            const float2 vm = prw[m];
+            const float gr = red[1 + 2 * m] + vm.x * v0r + vm.y * v0i;
+            const float gi = red[2 + 2 * m] + vm.x * v0i - vm.y * v0r;
             ctrl->gram[m][i] = make_float2(gr, gi);
           }
         }
@@ -514,26 +528,17 @@ __global__ void __launch_bounds__(kCNT, 1)
                          : (row > j && row < kw) ? x[pr][i] : (row == j ? v0s[i] : F32<T>::zero());
           if (row == j && refl) f_set(x[pr][i], -pr_ * xn, -pi_ * xn);
         }
-        // d_k = v_i^H x_k (k > i), then x_k -= tau d_k v_i
-        float dd[16];
-#pragma unroll
-        for (int a = 0; a < 16; ++a) dd[a] = 0.f;
-#pragma unroll
-        for (int pr = 0; pr < kPanelRP; ++pr) {
-#pragma unroll
-          for (int k = i + 1; k < kQB; ++k) {
-            float gr = 0.f, gi = 0.f;
-            f_dotc(vi[pr], x[pr][k], gr, gi);
-            dd[2 * k] += gr;
-            dd[2 * k + 1] += gi;
-          }
-        }
-        cta_sum(ctrl, dd, 2 * nbp);
+        // x_k -= tau d_k v_i, d_k = v_i^H x_k = (rows > j) + conj(v0_i) x_k[j]
 #pragma unroll
         for (int k = i + 1; k < kQB; ++k) {
-          const float wr = taus[i] * dd[2 * k], wi = taus[i] * dd[2 * k + 1];
+          if (k < nbp) {
+            const float2 xk = prw[k];
+            const float dr = red[2 * k - 1] + v0r * xk.x + v0i * xk.y;
+            const float di = red[2 * k] + v0r * xk.y - v0i * xk.x;
+            const float wr = taus[i] * dr, wi = taus[i] * di;
 #pragma unroll
-          for (int pr = 0; pr < kPanelRP; ++pr) f_axpy(wr, wi, vi[pr], x[pr][k]);
+            for (int pr = 0; pr < kPanelRP; ++pr) f_axpy(wr, wi, vi[pr], x[pr][k]);
+          }
         }
       }
     }
@@ -1039,6 +1044,14 @@ inline int e_bucket(int l) {
 
 }  // namespace
 
+// The sizes the cluster kernel takes (shared memory and registers aside).
+template <typename T>
+bool split_cluster_size_ok(int kw, int l) {
+  if (std::min(kw, l) > kMaxRows || kw > kCNT * kPanelRP) return false;
+  const int e = e_bucket(l);
+  return e != 0 && (sizeof(T) == sizeof(double) || e <= 16);
+}
+
 template <typename T>
 bool split_cluster_fits(int kw, int l) {
   // the QR panel holds kPanelRP rows per thread in registers
@@ -1085,6 +1098,8 @@ int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, do
   return SM_ERR_VALUE;
 }
 
+template bool split_cluster_size_ok<double>(int, int);
+template bool split_cluster_size_ok<cplx>(int, int);
 template bool split_cluster_fits<double>(int, int);
 template bool split_cluster_fits<cplx>(int, int);
 template int split_cluster_f32<double>(cudaStream_t, const double*, int, int, bool, double,

@@ -66,13 +66,27 @@ struct Sweeper {
 
   size_t site_elems(int i) const { return (size_t)bb[i] * d[i] * bb[i + 1]; }
 
+  // Sweep contractions in FP32 arithmetic: the mixed forms' setting, taken
+  // only when every two-site split of the sweep fits the FP32 cluster kernel.
+  // A split beyond it runs the FP64 Jacobi, which cannot deflate the FP32
+  // rounding noise of its input (singular values at 1e-7 of the largest
+  // instead of 1e-16): at n=40, chi=512 that made the FP64 splits 2.7x slower.
+  bool c32 = false;
+  void choose_contractions() {
+    c32 = ctx.precision != SM_PRECISION_FP64 && ctx.contract32;
+    for (int i = 0; c32 && i + 1 < L; ++i) {
+      const int M = cap[i] * d[i], N = d[i + 1] * cap[i + 2];
+      if (std::min(M, N) < kMixedMinRank) continue;  // FP64 path either way
+      c32 = split_cluster_size_ok<T>(N, M) && split_cluster_size_ok<T>(M, N);
+    }
+  }
+
   int buf(const std::string& name, size_t n, T** p) { return ctx.scratch(name, std::max<size_t>(n, 1), p); }
 
   // ---- helpers -------------------------------------------------------------
   int gemm_(int opA, int opB, int M, int N, int K, T alpha, const T* A, int lda, const T* B,
             int ldb, T beta, T* C, int ldc) {
-    if (ctx.precision != SM_PRECISION_FP64 && ctx.contract32)
-      return gemm_ctx_f32<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    if (c32) return gemm_ctx_f32<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
     return gemm_ctx<T>(ctx, st, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   }
   // FP64 contractions whatever the context's setting (norms and overlaps)
@@ -487,6 +501,7 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
       SM_CHECK(w.buf("sw.LA." + std::to_string(t), mla, &w.LA[t]));
       SM_CHECK(w.buf("sw.BR." + std::to_string(t), mbr, &w.BR[t]));
     }
+    w.choose_contractions();
     SM_CHECK(w.init_environments(start));
     double err = 2.0, nm = 0.0;
     int c = start;
@@ -509,14 +524,13 @@ int simplify_impl(Ctx& ctx, cudaStream_t st, int L, const int* phys, int nterms,
       if (err < s.simplification_tolerance || err > old_err) break;
       dir = -dir;
     }
-    if (ctx.contract32 && ctx.precision != SM_PRECISION_FP64) {
+    if (w.c32) {
       // the error bound's last term needs the overlap to FP64 accuracy: rebuild
       // the environments of the final centre with FP64 contractions
-      ctx.contract32 = false;
+      w.c32 = false;
       const int rc = w.init_environments(c);
       double sc = 0.0;
       const int rc2 = rc == SM_OK ? w.estimate(c, &nm, &sc) : rc;
-      ctx.contract32 = true;
       SM_CHECK(rc2);
       err = 2.0 * std::fabs(1.0 - sc / std::sqrt(nm * norm_state_sqr));
       if (rep->sweeps >= 1 && rep->sweeps <= 64) rep->sweep_err[rep->sweeps - 1] = err;
