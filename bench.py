@@ -607,7 +607,8 @@ def main():
                          "on the tensor cores (FP32 SIMT for small or complex shapes); the "
                          "state norm, the refinement and the final estimate stay FP64")
     ap.add_argument("--rank-model", default=None,
-                    help="trained rank predictor (.npz); trained here when absent")
+                    help="trained rank predictor (.npz); default: the packaged model "
+                         "(seemps2_gb300/data/rank_model.npz), else trained here")
     ap.add_argument("--train-count", type=int, default=90,
                     help="training workloads recorded when the predictor is trained here")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -685,9 +686,13 @@ def main():
         from seemps2_gb300 import learned
 
         t0 = time.perf_counter()
-        if args.rank_model and os.path.exists(args.rank_model):
-            model = learned.RankModel.load(args.rank_model)
-            learned_info = {"model": args.rank_model}
+        path = args.rank_model or learned.PACKAGED_MODEL
+        if path and os.path.exists(path):
+            model = learned.RankModel.load(path)
+            meta = np.load(path)
+            learned_info = {"model": os.path.relpath(path, ROOT),
+                            **{k: meta[k].item() for k in ("truncations", "workloads", "record_s",
+                                                           "train_s", "loss_last") if k in meta}}
         else:
             model, rep = learned.train_default(count=args.train_count, epochs=40, seed=1)
             learned_info = {"model": "trained in this run on the GPU (library kernels)", **rep}

@@ -1725,6 +1725,9 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // (noise of the sketch) a few more.  A deviation beyond kMixedOrthMax, or one
   // that a step did not reduce, means rows that the FP32 stage left nearly
   // parallel: the split goes to FP64.
+  // a capped QR (the predicted rank, or the range finder's k) that missed
+  // weight the rank needs is redone by the caller with the full QR
+  const bool capped = qr_cap > 0 && qr_cap < k;
   SM_CHECK(normalise(V));
   double e_ns = 0.0;
   bool ns_done = false;
@@ -1748,6 +1751,11 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
       ns_done = true;
       break;
     }
+  }
+  if (!ns_done && capped) {  // rows of a missed subspace: no use finishing this attempt
+    ctx.stats.mixed_cap_redone += 1;
+    *missed_out = true;
+    return SM_OK;
   }
   // 3. singular values, truncation, exact discarded weight
   SM_CHECK(w_vh(V, Cb));
@@ -1781,8 +1789,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // a capped QR that left weight the rank may need: more than 1% of what the
   // tolerance allows (and more than 1e-12 of |A|^2) outside the rows' span,
   // computed exactly after the refinement
-  const bool missed = qr_cap > 0 && qr_cap < k &&
-                      hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
+  const bool missed = capped && hs[5] > std::max(1e-12, 1e-2 * strat.tolerance) * norm2;
   const bool coupled = !(cut_angle <= kMixedCutAmp);
   const bool over_tol = r.err2 > allowed_discard(strat, norm2, s0, k, D) * (1.0 + 1e-12);
   const bool over = D < strat.max_bond_dimension && D < k && over_tol;
@@ -1790,9 +1797,10 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   // value leaves nothing to discard: either failing means the FP32 stage lost
   // directions, and the split goes to FP64.
   const bool lost = !ns_done || (D >= k && over_tol);
-  if ((missed || (over && qr_cap > 0 && qr_cap < k)) && !blind && !coupled && !lost) {
-    // the cap (or the QR's stop) left weight the rank needs: the caller
-    // retries with the full QR
+  if (capped && !blind && (missed || over || coupled || lost)) {
+    // the cap left weight the rank needs (then the rows span the wrong space
+    // and every later check may fail with it): the caller retries with the
+    // full QR; a split without a cap goes to FP64 instead
     ctx.stats.mixed_cap_redone += 1;
     *missed_out = true;
     return SM_OK;

@@ -21,6 +21,7 @@ installed, so the device sees raw features.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
 
 import numpy as np
@@ -28,6 +29,12 @@ import numpy as np
 from . import _lib
 
 DIMS = (_lib.RANK_FEATURES, 256, 256, 256, 1)
+
+# The predictor shipped with the package: trained on the GPU with the library's
+# kernels on truncations recorded by the FP64 method (``python -m
+# seemps2_gb300.learned --out ... --count 4300``; its record counts are stored
+# in the file).
+PACKAGED_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "rank_model.npz")
 
 
 def _torch():
@@ -245,12 +252,20 @@ def random_case(n, chi, D, rng, cplx):
 
 
 def training_workloads(rng, count: int):
-    """(mps, mpo, strategy kwargs) with the shapes the benchmarks use, small
-    sizes: Laplacian steps (tol 1e-12, max bond chi), random complex MPS x MPO
-    (tol 1e-10, max bond 2 chi), random real (tol 1e-8)."""
+    """(mps, mpo, strategy kwargs) with the shapes the benchmarks use: Laplacian
+    steps (tol 1e-12, max bond chi), random complex MPS x MPO (tol 1e-10, max
+    bond 2 chi), random real (tol 1e-8), mostly small; every 25th workload is a
+    Laplacian step of the benchmark's own scale (n 16..30, chi 128..256), so
+    that the bond caps and ranks of the timed workload lie inside the data."""
     for c in range(count):
         kind = c % 3
-        if kind == 0:
+        if c % 25 == 24:
+            n = int(rng.integers(16, 31))
+            chi = int(rng.choice([128, 192, 256]))
+            mps, mpo = laplacian_case(n, chi, rng)
+            kw = dict(tolerance=1e-12, max_bond_dimension=chi, max_sweeps=2,
+                      simplification_tolerance=0.0)
+        elif kind == 0:
             n = int(rng.integers(10, 24))
             chi = int(rng.choice([16, 32, 64, 96]))
             mps, mpo = laplacian_case(n, chi, rng)
@@ -309,8 +324,8 @@ def train_default(count: int = 60, epochs: int = 40, seed: int = 1, verbose: boo
     if verbose:
         print(f"recorded {len(D)} truncations in {t1 - t0:.1f} s; trained in {t2 - t1:.1f} s; "
               f"loss {hist[0]:.4f} -> {hist[-1]:.4f}")
-    return model, {"truncations": int(len(D)), "record_s": t1 - t0, "train_s": t2 - t1,
-                   "loss_first": hist[0], "loss_last": hist[-1]}
+    return model, {"truncations": int(len(D)), "workloads": int(count), "record_s": t1 - t0,
+                   "train_s": t2 - t1, "loss_first": hist[0], "loss_last": hist[-1]}
 
 
 def main():

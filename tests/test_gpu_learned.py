@@ -125,6 +125,24 @@ def test_trained_network_beats_the_baseline(trained):
     assert err_net < err_base, (err_net, err_base)
 
 
+def test_packaged_network_beats_the_baseline(trained):
+    """The predictor shipped in seemps2_gb300/data (trained on ~200k truncations of
+    the FP64 method) loads, and on held-out workloads its mean |error| in log2
+    rank is below the no-network baseline's and below 0.1 (7 % in the rank)."""
+    import os
+
+    *_, Xt, Dt = trained
+    assert os.path.exists(learned.PACKAGED_MODEL)
+    z = np.load(learned.PACKAGED_MODEL)
+    assert int(z["truncations"]) >= 200_000
+    model = learned.RankModel.load(learned.PACKAGED_MODEL)
+    model.install()
+    y = np.log2(np.maximum(Dt, 1))
+    err_net = np.mean(np.abs(model.predict_log2(Xt) - y))
+    err_base = np.mean(np.abs(learned.baseline_log2(Xt) - y))
+    assert err_net < err_base and err_net < 0.1, (err_net, err_base)
+
+
 def test_mixed_learned_apply_matches_oracle(trained):
     model, *_ = trained
     model.install()
