@@ -289,7 +289,7 @@ bool split_cluster_fits(int kw, int l);
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf);
+                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf, bool pivot = true);
 size_t split_cluster_vbuf_floats(int kw);
 
 }  // namespace sm

@@ -1598,8 +1598,10 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
       SM_CHECK(range_finder_bh(ctx, st, A, m, n, want_u, rf_k, ctx.rf_power, BH, rf_status));
       if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
       // BH (l x rf_k) is the cluster's W; A's own |A|^2 replaces |BH|^2 below
+      // no column pivoting here: W^T Q's columns come in the sketch's order, and
+      // pivoting them cost the range finder a redo per split (measured)
       SM_CHECK(split_cluster_f32<T>(st, BH, l, rf_k, false, thr_rel, thr_abs, 40, rows, nrm,
-                                    kcap, ctl, info, 0, vbuf));
+                                    kcap, ctl, info, 0, vbuf, false));
       if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
       SM_CHECK(vdot<T>(ctx, st, (size_t)m * n, A, A, a2));
       SM_CUDA_CHECK(cudaMemcpyAsync(info, a2, sizeof(double), cudaMemcpyDeviceToDevice, st));

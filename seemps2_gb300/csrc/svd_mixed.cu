@@ -192,6 +192,14 @@ struct CtrlS {
   float part[2][kCW][kQB];     // trailing-weight partials of all CTAs, by block-step parity
   float inpanel[kQB][kQB];     // owner of a panel: weight of panel column k below step i
   double part64[kCW];          // |W|^2 partials of all CTAs
+  float cn[64];                // remaining squared norm of each column slot (-1: not a candidate)
+  float cand_v[kCW][kQB];      // next panel's owner: every CTA's heaviest columns (value,
+  int cand_p[kCW][kQB];        //   position; -1: none)
+  int cand_n[kCW];             //   valid entries per CTA
+  int sel[kQB];                // next panel's owner: the chosen positions, heaviest first
+  int nsel;
+  int swp[2][kQB];             // next panel's owner: positions swapped (chosen, panel)
+  unsigned short perm[768];    // CTA 0: original column of each position
   float red[kCNW][kQB];        // CTA-local reduction scratch
   double red64[kCNW];
 };
@@ -251,7 +259,8 @@ __global__ void __launch_bounds__(kCNT, 1)
     k_split_cluster(const T* __restrict__ A, int n_a, int trans, int kw, int l, double thr_rel,
                     double thr_abs, float tol2, int max_sweeps, T* __restrict__ out_rows,
                     double* __restrict__ out_nrm, int kcap, JacobiCtl* ctl_out,
-                    double* __restrict__ info, int qr_cap, int qb, float* __restrict__ vbuf) {
+                    double* __restrict__ info, int qr_cap, int qb, float* __restrict__ vbuf,
+                    int pivot) {
   using F = typename F32<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
@@ -314,6 +323,18 @@ __global__ void __launch_bounds__(kCNT, 1)
     const int c = col_of(s);
     if (c >= l) break;
     for (int i = lane; i < kw; i += 32) cols[(size_t)s * ks + i] = F32<T>::from(Wat(i, c), scale);
+  }
+  if (rank == 0)
+    for (int c = tid; c < l; c += kCNT) ctrl->perm[c] = (unsigned short)c;
+  __syncthreads();
+  // squared column norms: the candidates for the first panel
+  for (int s = warp; s < 64; s += kCNW) {
+    const int c = s < ncs ? col_of(s) : l;
+    float a = 0.f;
+    if (c < l)
+      for (int i = lane; i < kw; i += 32) a += f_abs2(cols[(size_t)s * ks + i]);
+    a = warp_sum(a);
+    if (lane == 0) ctrl->cn[s] = c < l ? a : -1.f;
   }
   __syncthreads();
 
@@ -409,13 +430,18 @@ __global__ void __launch_bounds__(kCNT, 1)
       if (warp == 0) {
         float run = 0.f;  // S(nb-1) = the tail, S(i) = S(i+1) + |col[c0+i+1]|^2
         for (int w = 0; w < kCNW; ++w) run += tl[w * 32 + lane];
+        // the column's weight below the block, |col[c0+nb:kw)|^2: its pivot
+        // candidate value for the next panel
+        ctrl->cn[g * 32 + lane] = live ? run : -1.f;
+        float sv[kQB];  // this lane's S(i), then the nb independent warp sums
 #pragma unroll
         for (int i = kQB - 1; i >= 0; --i) {
-          if (i < nb) {
-            acc[i] += warp_sum(run);
-            if (i >= 1) run += ebin[i * 32 + lane];
-          }
+          sv[i] = i < nb ? run : 0.f;
+          if (i >= 1 && i < nb) run += ebin[i * 32 + lane];
         }
+#pragma unroll
+        for (int i = 0; i < kQB; ++i)
+          if (i < nb) acc[i] += warp_sum(sv[i]);
       }
       __syncthreads();
     }
@@ -634,8 +660,142 @@ __global__ void __launch_bounds__(kCNT, 1)
     __syncthreads();
   };
   auto slot_of = [&](int c) { return ((c / qb) / kCW) * qb + c % qb; };
-  // block 0: factored by CTA 0 before the first barrier
+  // Block column pivoting: the columns of the panel at positions cp ..
+  // cp+nbp-1 become the nbp live columns of largest remaining weight (cn, set
+  // from the columns' current values below row cp).  Every CTA sends its own
+  // heaviest nbp (value, position) to the panel's owner; after a cluster
+  // barrier the owner picks the heaviest nbp of all, swaps their column data
+  // (all kw rows) with the panel's positions over DSMEM and records the swaps
+  // in CTA 0's permutation.  The other CTAs wait at the step's barrier while
+  // their columns move.  All threads of all CTAs.
+  auto pivot_panel = [&](int cp, int nbp, int owner) {
+    CtrlS* co = cluster.map_shared_rank(ctrl, owner);
+    if (warp == 0) {  // this CTA's heaviest nbp slots, largest first (ties: smaller slot)
+      float v0 = lane < ncs ? ctrl->cn[lane] : -1.f;
+      float v1 = lane + 32 < ncs ? ctrl->cn[lane + 32] : -1.f;
+      int nv = 0;
+#pragma unroll 1
+      for (int k = 0; k < nbp; ++k) {
+        float bv = v0 >= v1 ? v0 : v1;
+        int bs = v0 >= v1 ? lane : lane + 32;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+          const int os = __shfl_xor_sync(0xffffffffu, bs, o);
+          if (ov > bv || (ov == bv && os < bs)) {
+            bv = ov;
+            bs = os;
+          }
+        }
+        if (bv < 0.f) break;  // uniform over the warp
+        if (lane == 0) {
+          co->cand_v[rank][k] = bv;
+          co->cand_p[rank][k] = col_of(bs);
+        }
+        ++nv;
+        if (bs == lane) v0 = -1.f;
+        else if (bs == lane + 32) v1 = -1.f;
+      }
+      if (lane == 0) co->cand_n[rank] = nv;
+    }
+    cluster.sync();
+    if (rank != owner) return;
+    if (warp == 0) {  // the heaviest nbp of the 16 x nbp candidates (ties: smaller position)
+      float v[4];
+      int pc[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int f = lane + 32 * u, c = f / kQB, k = f % kQB;
+        const bool ok = k < ctrl->cand_n[c];
+        v[u] = ok ? ctrl->cand_v[c][k] : -1.f;
+        pc[u] = ok ? ctrl->cand_p[c][k] : 0x7fffffff;
+      }
+      int ns = 0;
+#pragma unroll 1
+      for (int k = 0; k < nbp; ++k) {
+        float bv = v[0];
+        int bp = pc[0], bu = 0;
+#pragma unroll
+        for (int u = 1; u < 4; ++u)
+          if (v[u] > bv || (v[u] == bv && pc[u] < bp)) {
+            bv = v[u];
+            bp = pc[u];
+            bu = u;
+          }
+        int src = lane * 4 + bu;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+          const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+          const int os = __shfl_xor_sync(0xffffffffu, src, o);
+          if (ov > bv || (ov == bv && op < bp)) {
+            bv = ov;
+            bp = op;
+            src = os;
+          }
+        }
+        if (bv < 0.f) break;  // uniform over the warp
+        if (lane == 0) ctrl->sel[k] = bp;
+        ++ns;
+        if (src / 4 == lane) v[src % 4] = -1.f;
+      }
+      if (lane == 0) ctrl->nsel = ns;
+    }
+    __syncthreads();
+    const int nsel = ctrl->nsel;
+    // chosen columns already inside the panel stay; the others are paired in
+    // order with the panel positions that were not chosen
+    bool outside = false, freep = false;
+    if (tid < nsel) {
+      const int c = ctrl->sel[tid];
+      outside = c < cp || c >= cp + nbp;
+    }
+    if (tid >= 32 && tid < 32 + nbp) {
+      const int pp = cp + tid - 32;
+      freep = true;
+      for (int k = 0; k < nsel; ++k) freep = freep && ctrl->sel[k] != pp;
+    }
+    const int ns = __syncthreads_count(outside);
+    if (outside) {
+      int oi = 0;
+      for (int k = 0; k < tid; ++k) {
+        const int c = ctrl->sel[k];
+        oi += (c < cp || c >= cp + nbp) ? 1 : 0;
+      }
+      ctrl->swp[0][oi] = ctrl->sel[tid];
+    }
+    if (freep) {
+      int fi = 0;
+      for (int j = 0; j < tid - 32; ++j) {
+        bool f = true;
+        for (int k = 0; k < nsel; ++k) f = f && ctrl->sel[k] != cp + j;
+        fi += f ? 1 : 0;
+      }
+      if (fi < ns) ctrl->swp[1][fi] = cp + tid - 32;
+    }
+    __syncthreads();
+    // swap the column data: pair k, row i for f = k * kw + i (independent items)
+    for (int f = tid; f < ns * kw; f += kCNT) {
+      const int k = f / kw, i = f % kw;
+      const int a = ctrl->swp[0][k], b = ctrl->swp[1][k];
+      F* pa = cluster.map_shared_rank(cols + (size_t)slot_of(a) * ks, (a / qb) % kCW);
+      F* pb = cols + (size_t)slot_of(b) * ks;  // the panel's positions are the owner's
+      const F ta = pa[i];
+      pa[i] = pb[i];
+      pb[i] = ta;
+    }
+    if (tid < ns) {
+      unsigned short* pm = cluster.map_shared_rank(ctrl, 0)->perm;
+      const int a = ctrl->swp[0][tid], b = ctrl->swp[1][tid];
+      const unsigned short t = pm[a];
+      pm[a] = pm[b];
+      pm[b] = t;
+    }
+    __syncthreads();
+  };
+  // block 0: pivoted and factored by CTA 0 before the first step's barrier
   const int nb0 = min(qb, qsteps);
+  if (pivot && nb0 > 0) pivot_panel(0, nb0, 0);
   if (rank == 0 && nb0 > 0) {
     factor_panel(0, nb0, 0, 0);
     __syncthreads();
@@ -661,7 +821,8 @@ __global__ void __launch_bounds__(kCNT, 1)
 #pragma unroll
       for (int i = 0; i < kQB; ++i) ctrl->red[0][i] = acc[i];
     }
-    // the next panel, now up to date
+    // the next panel: its columns chosen by weight, now up to date
+    if (pivot && nb1 > 0) pivot_panel(c1, nb1, (q + 1) % kCW);
     if (owner1) {
       factor_panel(c1, nb1, sp1, par ^ 1);
       __syncthreads();
@@ -925,6 +1086,7 @@ __global__ void __launch_bounds__(kCNT, 1)
   }
 
   // ---- phase 4: rows back to global memory (FP64, rescaled) ------------------
+  const unsigned short* perm0 = cluster.map_shared_rank(ctrl, 0)->perm;
   for (int j = warp; j < 2 * r; j += kCNW) {
     const int row = (j < r ? rank : 2 * kCW - 1 - rank) * r + (j % r);
     if (row >= kcap) continue;
@@ -932,10 +1094,10 @@ __global__ void __launch_bounds__(kCNT, 1)
     double acc = 0.0;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int c = lane + 32 * e;
+      const int c = lane + 32 * e;  // a position of the pivoted QR: column perm[c] of W
       if (c < l) {
         const T x = F32<T>::to(src[c], nrm);
-        out_rows[(size_t)row * l + c] = x;
+        out_rows[(size_t)row * l + perm0[c]] = x;
         acc += S<T>::abs2(x);
       }
     }
@@ -1003,7 +1165,7 @@ template <typename T, int E>
 int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw, int l,
                          double thr_rel, double thr_abs, int max_sweeps, T* out_rows,
                          double* out_nrm, int kcap, JacobiCtl* ctl, double* info, int qr_cap,
-                         float* vbuf) {
+                         float* vbuf, int pivot) {
   size_t smem = 0;
   int qb = 0;
   if (!cluster_config<T, E>(kw, l, &smem, &qb)) {
@@ -1026,7 +1188,7 @@ int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw
   const float tol2 = (float)l * eps * eps;
   SM_CUDA_CHECK(cudaLaunchKernelEx(&cfg, k_split_cluster<T, E>, A, n_a, trans, kw, l, thr_rel,
                                    thr_abs, tol2, max_sweeps, out_rows, out_nrm, kcap, ctl,
-                                   info, qr_cap, qb, vbuf));
+                                   info, qr_cap, qb, vbuf, pivot));
   note_launch();
   return SM_OK;
 }
@@ -1075,7 +1237,7 @@ bool split_cluster_fits(int kw, int l) {
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf) {
+                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf, bool pivot) {
   // W = A^T (kw = n, l = m) when U is wanted, else W = A (kw = m, l = n)
   const int kw = want_u ? n : m;
   const int l = want_u ? m : n;
@@ -1084,7 +1246,8 @@ int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, do
 #define SM_C(EV)                                                                              \
   case EV:                                                                                    \
     return launch_split_cluster<T, EV>(st, A, n, trans, kw, l, thr_rel, thr_abs, max_sweeps, \
-                                       out_rows, out_nrm, kcap, ctl, info, qr_cap, vbuf)
+                                       out_rows, out_nrm, kcap, ctl, info, qr_cap, vbuf,  \
+                                       pivot ? 1 : 0)
     SM_C(4);
     SM_C(8);
     SM_C(12);
@@ -1104,9 +1267,10 @@ template bool split_cluster_fits<double>(int, int);
 template bool split_cluster_fits<cplx>(int, int);
 template int split_cluster_f32<double>(cudaStream_t, const double*, int, int, bool, double,
                                        double, int, double*, double*, int, JacobiCtl*, double*,
-                                       int, float*);
+                                       int, float*, bool);
 template int split_cluster_f32<cplx>(cudaStream_t, const cplx*, int, int, bool, double, double,
-                                     int, cplx*, double*, int, JacobiCtl*, double*, int, float*);
+                                     int, cplx*, double*, int, JacobiCtl*, double*, int, float*,
+                                     bool);
 
 size_t split_cluster_vbuf_floats(int kw) {
   // two parities of a reflector block [kwp][8] and its T [8][8], complex

@@ -139,7 +139,7 @@ def test_mixed_split_against_oracle(mixed, cplx, case, side):
 @pytest.mark.parametrize("want_u", [0, 1])
 @pytest.mark.parametrize("shape", [(96, 64), (64, 200), (320, 320), (512, 256)])
 def test_cluster_rows_span_and_orthogonality(cplx, want_u, shape):
-    """FP32 stage alone: rows mutually orthogonal to FP32 accuracy, Y^H Y = W^H W
+    """FP32 stage alone: rows mutually orthogonal to the stop rule's level, Y^H Y = W^H W
     (same row space and singular values) to FP32 accuracy."""
     import ctypes as C
 
@@ -173,11 +173,13 @@ def test_cluster_rows_span_and_orthogonality(cplx, want_u, shape):
     # singular values = row norms (sorted), to FP32 backward error of |W|_F
     sv = np.sort(nv)[::-1][: len(s)]
     assert np.abs(sv - s).max() <= 2e-5 * np.linalg.norm(W)
-    # mutual orthogonality of the significant rows
+    # mutual orthogonality of the significant rows: the Jacobi stops after a
+    # sweep whose rotations all started below cosine 1e-2, so about 1e-4 is left
+    # for the FP64 refinement
     big = nv > 1e-4
     Yb = Y[big] / nv[big, None]
     off = Yb.conj() @ Yb.T - np.eye(big.sum())
-    assert np.abs(off).max() <= 1e-4
+    assert np.abs(off).max() <= 1e-3
 
 
 def test_mixed_zero_matrix(mixed):
