@@ -64,6 +64,8 @@ struct Ctx {
   std::vector<double> prev_s;
   const double* last_s = nullptr;  // device: sorted singular values of the last split
   int last_len = 0;
+  double* prev_s_dev = nullptr;     // device copy of the last split's 32 largest values
+  int prev_len_dev = 0;             //   (the learned form's features, read on the device)
   RankModel model;
   bool record = false;
   std::vector<float> rec_x;
@@ -129,6 +131,8 @@ struct JacobiCtl {
   int sweeps;
   int nact;  // rows still taking part in the iteration (deflation / rank)
   int nkeep;  // mixed split: FP32 rows heavy enough to take into the FP64 refinement
+  int cap;    // mixed split: the QR cap the cluster kernel used (0: none)
+  int pred;   // mixed split: the predicted rank behind a device-side cap (0: none)
 };
 
 // Output forms of the two factors of a split A = U diag(s) Vt.
@@ -269,6 +273,11 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
 void rank_features(const Ctx& ctx, int k, const sm_strategy& st, float* f);
 // Kept rank of that split predicted by the context's model (1..k).
 int rank_predict(Ctx& ctx, cudaStream_t st, int k, const sm_strategy& strat, int* out);
+// The same prediction without a host round trip: features from the previous
+// split's values on the device, the network, and the QR cap it gives,
+// out[0] = cap (0 when above useful min(m, n)), out[1] = the predicted rank.
+int rank_predict_dev(Ctx& ctx, cudaStream_t st, int k, const sm_strategy& strat, double useful,
+                     int* out);
 
 // --- svd_mixed.cu ------------------------------------------------------------
 // Whether the 16-CTA cluster factorisation holds W (kw x l) on this GPU.
@@ -289,7 +298,8 @@ bool split_cluster_fits(int kw, int l);
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf, bool pivot = true);
+                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf, bool pivot = true,
+                      const int* cap_dev = nullptr);
 size_t split_cluster_vbuf_floats(int kw);
 
 }  // namespace sm

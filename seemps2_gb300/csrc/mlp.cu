@@ -244,6 +244,39 @@ int infer(Ctx& c, cudaStream_t st, float* X, int batch, float* tmp, float** out)
   return SM_OK;
 }
 
+// The features of rank_features on the device: f[0..31] from the previous
+// split's sorted values (len of them), then the host-known scalars.
+__global__ void k_rank_features(const double* __restrict__ prev_s, int len, float site,
+                                float ltol, float lprev, float lk, float lmaxb,
+                                float* __restrict__ f) {
+  const int i = threadIdx.x;
+  if (i < 32) {
+    float v = -20.f;
+    if (prev_s && i < len) {
+      const double s0 = prev_s[0], si = prev_s[i];
+      if (s0 > 0.0 && si > 0.0) v = (float)fmax(-20.0, log10(si / s0));
+    }
+    f[i] = v;
+  } else if (i == 32) {
+    f[32] = site;
+    f[33] = ltol;
+    f[34] = lprev;
+    f[35] = lk;
+    f[36] = lmaxb;
+  }
+}
+
+// The QR cap from the network's log2-rank output y: r = clamp(ceil(2^y), 1, k),
+// cap = min(k, ceil(margin r) + extra), 0 when it exceeds useful k.
+__global__ void k_rank_cap(const float* __restrict__ y, int k, double margin, int extra,
+                           double useful, int* __restrict__ out) {
+  const double r = fmin((double)k, fmax(1.0, ceil(exp2((double)y[0]))));
+  int cap = (int)fmin((double)k, ceil(margin * r) + extra);
+  if (cap > useful * k) cap = 0;
+  out[0] = cap;
+  out[1] = (int)r;
+}
+
 }  // namespace
 
 // ---- rank features --------------------------------------------------------
@@ -261,6 +294,31 @@ void rank_features(const Ctx& ctx, int k, const sm_strategy& st, float* f) {
   f[34] = (float)std::log2(1.0 + ctx.prev_rank);
   f[35] = (float)std::log2((double)std::max(1, k));
   f[36] = (float)std::log2((double)std::min(std::max(1, st.max_bond_dimension), 1 << 20));
+}
+
+int rank_predict_dev(Ctx& ctx, cudaStream_t st, int k, const sm_strategy& strat, double useful,
+                     int* out) {
+  if (!ctx.model.loaded) {
+    set_error("rank model not set");
+    return SM_ERR_VALUE;
+  }
+  float* x;
+  SM_CHECK(ctx.scratch("mlp.infer", (size_t)3 * 4096, &x));
+  const float site = ctx.split_n > 0 ? (float)ctx.split_site / (float)ctx.split_n : 0.5f;
+  const float ltol = strat.tolerance > 0.0 ? (float)std::log10(strat.tolerance) : -20.f;
+  const float lprev = (float)std::log2(1.0 + ctx.prev_rank);
+  const float lk = (float)std::log2((double)std::max(1, k));
+  const float lmaxb =
+      (float)std::log2((double)std::min(std::max(1, strat.max_bond_dimension), 1 << 20));
+  k_rank_features<<<1, 64, 0, st>>>(ctx.prev_len_dev > 0 ? ctx.prev_s_dev : nullptr,
+                                    ctx.prev_len_dev, site, ltol, lprev, lk, lmaxb, x);
+  note_launch();
+  float* y = nullptr;
+  SM_CHECK(infer(ctx, st, x, 1, x + 4096, &y));
+  k_rank_cap<<<1, 1, 0, st>>>(y, k, ctx.cap_margin, ctx.cap_extra, useful, out);
+  note_launch();
+  SM_CUDA_CHECK(cudaGetLastError());
+  return SM_OK;
 }
 
 // Kept rank of a split of size k predicted by the context's model (1..k).

@@ -1530,7 +1530,7 @@ double allowed_discard(const sm_strategy& st, double norm2, double s0, int k, in
 template <typename T>
 int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_strategy& strat,
                     bool want_u, T* left, T* right, SplitResult* out, bool* done, int qr_cap,
-                    bool* missed_out, int rf_k = 0) {
+                    bool* missed_out, int rf_k = 0, const int* cap_dev = nullptr) {
   *done = false;
   *missed_out = false;
   const int kw = want_u ? n : m;
@@ -1610,7 +1610,7 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   if (rf_k == 0) {
     if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev0, st));
     SM_CHECK(split_cluster_f32<T>(st, A, m, n, want_u, thr_rel, thr_abs, 40, rows, nrm, kcap, ctl,
-                                  info, qr_cap, vbuf));
+                                  info, qr_cap, vbuf, true, cap_dev));
     if (ctx.timing) SM_CUDA_CHECK(cudaEventRecord(ctx.ev1, st));
   }
   struct Head {
@@ -1631,6 +1631,12 @@ int svd_split_mixed(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const s
   SM_CUDA_CHECK(cudaStreamSynchronize(st));
   const double norm2 = h->info[0];  // the pinned block is reused below
   const JacobiCtl hc = h->c;
+  if (cap_dev) {  // the cap the predictor set on the device, now known here
+    qr_cap = hc.cap;
+    if (qr_cap > 0) ctx.stats.mixed_capped += 1;
+    ctx.stats.rank_predicted_sum += hc.pred;
+    ctx.stats.rank_predictions += 1;
+  }
   ctx.stats.mixed_splits += 1;
   ctx.stats.cluster_qr_ms += h->info[5];
   ctx.stats.cluster_jacobi_ms += h->info[6];
@@ -1852,10 +1858,21 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
   const bool xv = left_mode == OUT_US && right_mode == OUT_VT;
   if ((xu || xv) && ctx.precision != SM_PRECISION_FP64 && !s_out) {
     int cap = 0, rf_k = 0;
+    const int* cap_dev = nullptr;
     const bool hint = ctx.range_finder && ctx.rf_rank_hint > 0;
-    if (ctx.precision == SM_PRECISION_MIXED_LEARNED && (ctx.model.loaded || hint) &&
-        std::min(m, n) >= kMixedMinRank && strat.method == SM_RELATIVE_NORM_SQUARED_ERROR &&
-        strat.tolerance >= kMixedMinTol) {
+    const bool learned = ctx.precision == SM_PRECISION_MIXED_LEARNED &&
+                         std::min(m, n) >= kMixedMinRank &&
+                         strat.method == SM_RELATIVE_NORM_SQUARED_ERROR &&
+                         strat.tolerance >= kMixedMinTol;
+    if (learned && !ctx.range_finder && ctx.model.loaded) {
+      // the cap stays on the device: features, network and cap without a host
+      // round trip; the cluster kernel reads it (the host learns it with the
+      // kernel's other results)
+      int* d_cap;
+      SM_CHECK(ctx.scratch("rank.cap", 2, &d_cap));
+      SM_CHECK(rank_predict_dev(ctx, st, std::min(m, n), strat, kCapUseful, d_cap));
+      cap_dev = d_cap;
+    } else if (learned && (ctx.model.loaded || hint)) {
       int r = ctx.rf_rank_hint;
       if (!hint) SM_CHECK(rank_predict(ctx, st, std::min(m, n), strat, &r));
       cap = std::min(std::min(m, n), (int)std::ceil(ctx.cap_margin * r) + ctx.cap_extra);
@@ -1870,7 +1887,7 @@ static int svd_split_run(Ctx& ctx, cudaStream_t st, const T* A, int m, int n,
     }
     bool done = false, missed = false;
     SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done, cap,
-                                &missed, rf_k));
+                                &missed, rf_k, cap_dev));
     if (done) return SM_OK;
     if (missed)  // predicted rank too small: the full QR
       SM_CHECK(svd_split_mixed<T>(ctx, st, A, m, n, strat, xu, left, right, out, &done,
@@ -2018,8 +2035,17 @@ int svd_split(Ctx& ctx, cudaStream_t st, const T* A, int m, int n, const sm_stra
     }
     ctx.prev_rank = out->D;
     const int c = std::min(32, ctx.last_len);
-    ctx.prev_s.assign(c, 0.0);
+    // the next split's features: on the device for the device-side predictor
+    // (no host round trip), on the host when recording or predicting there
+    ctx.prev_len_dev = 0;
     if (c > 0 && ctx.last_s) {
+      SM_CHECK(ctx.scratch("rank.prev_s", 32, &ctx.prev_s_dev));
+      SM_CUDA_CHECK(cudaMemcpyAsync(ctx.prev_s_dev, ctx.last_s, sizeof(double) * c,
+                                    cudaMemcpyDeviceToDevice, st));
+      ctx.prev_len_dev = c;
+    }
+    ctx.prev_s.assign(c, 0.0);
+    if (c > 0 && ctx.last_s && (ctx.record || ctx.range_finder || !ctx.model.loaded)) {
       SM_CUDA_CHECK(cudaMemcpyAsync(ctx.prev_s.data(), ctx.last_s, sizeof(double) * c,
                                     cudaMemcpyDeviceToHost, st));
       SM_CUDA_CHECK(cudaStreamSynchronize(st));

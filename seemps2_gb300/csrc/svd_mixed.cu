@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(kCNT, 1)
                     double thr_abs, float tol2, int max_sweeps, T* __restrict__ out_rows,
                     double* __restrict__ out_nrm, int kcap, JacobiCtl* ctl_out,
                     double* __restrict__ info, int qr_cap, int qb, float* __restrict__ vbuf,
-                    int pivot) {
+                    int pivot, const int* __restrict__ cap_dev) {
   using F = typename F32<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
@@ -271,7 +271,9 @@ __global__ void __launch_bounds__(kCNT, 1)
   // ((c / qb) / 16) qb + c % qb
   const int ncs = qr_slots(l, qb);  // column slots per CTA
   const int kmax = min(kw, l);
-  // a learned rank caps the QR steps (0: the trailing weight alone decides)
+  // a learned rank caps the QR steps (0: the trailing weight alone decides);
+  // a cap computed on the device by the rank predictor replaces qr_cap
+  if (cap_dev) qr_cap = cap_dev[0];
   const int qsteps = qr_cap > 0 ? min(kmax, qr_cap) : kmax;
   constexpr int LP = 32 * E;
 
@@ -1113,6 +1115,8 @@ __global__ void __launch_bounds__(kCNT, 1)
     ctl_out->status = status;
     ctl_out->sweeps = sweeps;
     ctl_out->nact = keff;
+    ctl_out->cap = qr_cap;
+    ctl_out->pred = cap_dev ? cap_dev[1] : 0;
     info[0] = norm2;
     info[1] = (double)trail * norm2;
     info[5] = 1e-6 * (double)(t_qr - t_start);       // ms: load + QR
@@ -1165,7 +1169,7 @@ template <typename T, int E>
 int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw, int l,
                          double thr_rel, double thr_abs, int max_sweeps, T* out_rows,
                          double* out_nrm, int kcap, JacobiCtl* ctl, double* info, int qr_cap,
-                         float* vbuf, int pivot) {
+                         float* vbuf, int pivot, const int* cap_dev) {
   size_t smem = 0;
   int qb = 0;
   if (!cluster_config<T, E>(kw, l, &smem, &qb)) {
@@ -1188,7 +1192,7 @@ int launch_split_cluster(cudaStream_t st, const T* A, int n_a, int trans, int kw
   const float tol2 = (float)l * eps * eps;
   SM_CUDA_CHECK(cudaLaunchKernelEx(&cfg, k_split_cluster<T, E>, A, n_a, trans, kw, l, thr_rel,
                                    thr_abs, tol2, max_sweeps, out_rows, out_nrm, kcap, ctl,
-                                   info, qr_cap, qb, vbuf, pivot));
+                                   info, qr_cap, qb, vbuf, pivot, cap_dev));
   note_launch();
   return SM_OK;
 }
@@ -1237,7 +1241,8 @@ bool split_cluster_fits(int kw, int l) {
 template <typename T>
 int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, double thr_rel,
                       double thr_abs, int max_sweeps, T* out_rows, double* out_nrm, int kcap,
-                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf, bool pivot) {
+                      JacobiCtl* ctl, double* info, int qr_cap, float* vbuf, bool pivot,
+                      const int* cap_dev) {
   // W = A^T (kw = n, l = m) when U is wanted, else W = A (kw = m, l = n)
   const int kw = want_u ? n : m;
   const int l = want_u ? m : n;
@@ -1247,7 +1252,7 @@ int split_cluster_f32(cudaStream_t st, const T* A, int m, int n, bool want_u, do
   case EV:                                                                                    \
     return launch_split_cluster<T, EV>(st, A, n, trans, kw, l, thr_rel, thr_abs, max_sweeps, \
                                        out_rows, out_nrm, kcap, ctl, info, qr_cap, vbuf,  \
-                                       pivot ? 1 : 0)
+                                       pivot ? 1 : 0, cap_dev)
     SM_C(4);
     SM_C(8);
     SM_C(12);
@@ -1267,10 +1272,10 @@ template bool split_cluster_fits<double>(int, int);
 template bool split_cluster_fits<cplx>(int, int);
 template int split_cluster_f32<double>(cudaStream_t, const double*, int, int, bool, double,
                                        double, int, double*, double*, int, JacobiCtl*, double*,
-                                       int, float*, bool);
+                                       int, float*, bool, const int*);
 template int split_cluster_f32<cplx>(cudaStream_t, const cplx*, int, int, bool, double, double,
                                      int, cplx*, double*, int, JacobiCtl*, double*, int, float*,
-                                     bool);
+                                     bool, const int*);
 
 size_t split_cluster_vbuf_floats(int kw) {
   // two parities of a reflector block [kwp][8] and its T [8][8], complex

@@ -59,6 +59,7 @@ struct Sweeper {
   // each call starts the split features afresh (no previous split)
   Sweeper(Ctx& c, cudaStream_t stream, const sm_strategy& strat) : ctx(c), st(stream), s(strat) {
     ctx.prev_s.clear();
+    ctx.prev_len_dev = 0;
     ctx.prev_rank = 0;
     ctx.split_site = -1;
     ctx.split_n = 0;
