@@ -20,7 +20,12 @@
 //            shared-memory broadcast); then the CTA owning the next block
 //            factors that block's columns (its "panel") with all its threads:
 //            each holds two rows of the panel in registers, and a reflector
-//            costs two CTA-wide sums.  The owner writes the reflector block
+//            costs one CTA-wide sum.  Before that, block column pivoting puts
+//            the 8 live columns of largest remaining weight into the panel's
+//            positions (every CTA sends its heaviest to the owner, which
+//            swaps the winners' data in over DSMEM and records the swap in
+//            CTA 0's permutation; phase 4 undoes it).  The owner writes the
+//            reflector block
 //            and its T factor once to global memory; after the barrier every
 //            other CTA copies them from L2 into its shared memory (a DSMEM
 //            broadcast from one SM to 15 is bound by that SM's outgoing
@@ -38,8 +43,9 @@
 //            pairs, one warp per pair, CTA barriers only) and passes its
 //            blocks to the neighbouring CTAs through double-buffered DSMEM
 //            mailboxes.  One cluster barrier per block round (31 per sweep).
-//   phase 4  the rows (= diag(s) V^H of the rows of R, i.e. of W) go back to
-//            global memory in FP64, rescaled by |W|_F, with their FP64 norms.
+//   phase 4  the rows (= diag(s) V^H of the rows of R, i.e. of W, in W's own
+//            column order) go back to global memory in FP64, rescaled by
+//            |W|_F, with their FP64 norms.
 //
 // Only the accuracy of the iteration changes: the rows of V^H are accurate
 // to FP32 rounding.  The caller re-orthonormalises them in FP64 and forms the
