@@ -681,7 +681,8 @@ __global__ void __launch_bounds__(kCNT, 1)
     if (warp == 0) {  // this CTA's heaviest nbp slots, largest first (ties: smaller slot)
       float v0 = lane < ncs ? ctrl->cn[lane] : -1.f;
       float v1 = lane + 32 < ncs ? ctrl->cn[lane + 32] : -1.f;
-      int nv = 0;
+      float myv = -1.f;  // lane k keeps the k-th result
+      int myp = -1, nv = 0;
 #pragma unroll 1
       for (int k = 0; k < nbp; ++k) {
         float bv = v0 >= v1 ? v0 : v1;
@@ -696,56 +697,53 @@ __global__ void __launch_bounds__(kCNT, 1)
           }
         }
         if (bv < 0.f) break;  // uniform over the warp
-        if (lane == 0) {
-          co->cand_v[rank][k] = bv;
-          co->cand_p[rank][k] = col_of(bs);
+        if (lane == k) {
+          myv = bv;
+          myp = col_of(bs);
         }
         ++nv;
         if (bs == lane) v0 = -1.f;
         else if (bs == lane + 32) v1 = -1.f;
       }
+      // one store per array to the owner (lanes k < nv)
+      if (lane < nv) {
+        co->cand_v[rank][lane] = myv;
+        co->cand_p[rank][lane] = myp;
+      }
       if (lane == 0) co->cand_n[rank] = nv;
     }
     cluster.sync();
     if (rank != owner) return;
-    if (warp == 0) {  // the heaviest nbp of the 16 x nbp candidates (ties: smaller position)
-      float v[4];
-      int pc[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int f = lane + 32 * u, c = f / kQB, k = f % kQB;
-        const bool ok = k < ctrl->cand_n[c];
-        v[u] = ok ? ctrl->cand_v[c][k] : -1.f;
-        pc[u] = ok ? ctrl->cand_p[c][k] : 0x7fffffff;
-      }
+    if (warp == 0) {  // merge of the 16 descending lists: lane c holds list c's head
+      const int c = lane & (kCW - 1);
+      const int nc = ctrl->cand_n[c];
+      int head = 0;
+      float hv = (lane < kCW && nc > 0) ? ctrl->cand_v[c][0] : -1.f;
+      int hp = (lane < kCW && nc > 0) ? ctrl->cand_p[c][0] : 0x7fffffff;
       int ns = 0;
 #pragma unroll 1
       for (int k = 0; k < nbp; ++k) {
-        float bv = v[0];
-        int bp = pc[0], bu = 0;
+        float bv = hv;
+        int bp = hp, bl = lane;
 #pragma unroll
-        for (int u = 1; u < 4; ++u)
-          if (v[u] > bv || (v[u] == bv && pc[u] < bp)) {
-            bv = v[u];
-            bp = pc[u];
-            bu = u;
-          }
-        int src = lane * 4 + bu;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
+        for (int o = 16; o > 0; o >>= 1) {  // largest value, then smallest position
           const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
           const int op = __shfl_xor_sync(0xffffffffu, bp, o);
-          const int os = __shfl_xor_sync(0xffffffffu, src, o);
+          const int ol = __shfl_xor_sync(0xffffffffu, bl, o);
           if (ov > bv || (ov == bv && op < bp)) {
             bv = ov;
             bp = op;
-            src = os;
+            bl = ol;
           }
         }
         if (bv < 0.f) break;  // uniform over the warp
         if (lane == 0) ctrl->sel[k] = bp;
         ++ns;
-        if (src / 4 == lane) v[src % 4] = -1.f;
+        if (lane == bl) {  // the winning list advances
+          ++head;
+          hv = head < nc ? ctrl->cand_v[c][head] : -1.f;
+          hp = head < nc ? ctrl->cand_p[c][head] : 0x7fffffff;
+        }
       }
       if (lane == 0) ctrl->nsel = ns;
     }
@@ -782,15 +780,26 @@ __global__ void __launch_bounds__(kCNT, 1)
       if (fi < ns) ctrl->swp[1][fi] = cp + tid - 32;
     }
     __syncthreads();
-    // swap the column data: pair k, row i for f = k * kw + i (independent items)
-    for (int f = tid; f < ns * kw; f += kCNT) {
-      const int k = f / kw, i = f % kw;
-      const int a = ctrl->swp[0][k], b = ctrl->swp[1][k];
-      F* pa = cluster.map_shared_rank(cols + (size_t)slot_of(a) * ks, (a / qb) % kCW);
-      F* pb = cols + (size_t)slot_of(b) * ks;  // the panel's positions are the owner's
-      const F ta = pa[i];
-      pa[i] = pb[i];
+    // swap the column data: pair k, row i for f = k * kw + i (independent
+    // items), two per thread at a time so that their DSMEM loads overlap
+    for (int f = tid; f < ns * kw; f += 2 * kCNT) {
+      const int g = f + kCNT;
+      const bool two = g < ns * kw;
+      const int k = f / kw, i = f % kw, k2 = two ? g / kw : k, i2 = two ? g % kw : i;
+      F* pa = cluster.map_shared_rank(cols + (size_t)slot_of(ctrl->swp[0][k]) * ks,
+                                      (ctrl->swp[0][k] / qb) % kCW);
+      F* pa2 = cluster.map_shared_rank(cols + (size_t)slot_of(ctrl->swp[0][k2]) * ks,
+                                       (ctrl->swp[0][k2] / qb) % kCW);
+      F* pb = cols + (size_t)slot_of(ctrl->swp[1][k]) * ks;  // the panel's positions are the owner's
+      F* pb2 = cols + (size_t)slot_of(ctrl->swp[1][k2]) * ks;
+      const F ta = pa[i], ta2 = pa2[i2];
+      const F tb = pb[i], tb2 = pb2[i2];
+      pa[i] = tb;
       pb[i] = ta;
+      if (two) {
+        pa2[i2] = tb2;
+        pb2[i2] = ta2;
+      }
     }
     if (tid < ns) {
       unsigned short* pm = cluster.map_shared_rank(ctrl, 0)->perm;
