@@ -182,6 +182,41 @@ def test_cluster_rows_span_and_orthogonality(cplx, want_u, shape):
     assert np.abs(off).max() <= 1e-3
 
 
+@pytest.mark.parametrize("cplx", [False, True])
+def test_cluster_qr_pivots_heavy_columns_first(cplx):
+    """Block column pivoting in the FP32 QR: W (256 x 256) whose first 192
+    columns are zero and whose last 64 hold a rank-24 matrix.  Every panel takes
+    the heaviest remaining columns, so the rank-revealing QR stops within a few
+    blocks of the rank (keff <= 40; unpivoted it would first step through the
+    192 zero columns), and the rows still give W's Gram matrix and singular
+    values, in W's own column order."""
+    import ctypes as C
+
+    rng = np.random.default_rng(4)
+    m = n = 256
+    s = np.geomspace(1.0, 1e-2, 24)
+    A = np.zeros((m, n), complex if cplx else float)
+    A[:, 192:] = spectrum_matrix(rng, m, 64, s, cplx)
+    kcap = n + 32
+    dt = torch.complex128 if cplx else torch.float64
+    Ad = torch.from_numpy(np.ascontiguousarray(A)).to("cuda")
+    rows = torch.empty(kcap, n, dtype=dt, device="cuda")
+    nrm = torch.empty(kcap, dtype=torch.float64, device="cuda")
+    keff, sweeps = C.c_int(), C.c_int()
+    _lib.check(_lib.load().sm_split_rows_f32(
+        _lib.context(), 1 if cplx else 0, _lib.ptr(Ad), m, n, 0, 1e-14, 0.0, _lib.ptr(rows),
+        C.cast(nrm.data_ptr(), C.POINTER(C.c_double)), kcap, C.byref(keff), C.byref(sweeps),
+        _lib.stream_handle()))
+    torch.cuda.synchronize()
+    assert 24 <= keff.value <= 40, keff.value
+    Y = rows.cpu().numpy()
+    nv = nrm.cpu().numpy()
+    assert np.abs(Y.conj().T @ Y - A.conj().T @ A).max() <= 1e-5 * np.linalg.norm(A) ** 2
+    assert np.abs(Y[:, :192]).max() == 0.0  # the zero columns stay zero, in place
+    sv = np.sort(nv)[::-1][:24]
+    assert np.abs(sv - s).max() <= 2e-5 * np.linalg.norm(A)
+
+
 def test_mixed_zero_matrix(mixed):
     AA = np.zeros((16, 2, 2, 16))
     L, R, err = core._left_orth_2site(AA, sg.Strategy(tolerance=1e-10))
