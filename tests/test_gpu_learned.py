@@ -169,6 +169,38 @@ def test_mixed_learned_apply_matches_oracle(trained):
     assert fe < 1e-10, fe
 
 
+def test_device_prediction_matches_host_features(trained):
+    """The learned form predicts on the device (features from the previous
+    split's values kept on the device, the network, the cap) with no host round
+    trip.  Recording the same apply gives the host-side features of every
+    split: the network on those (host side) must give the same ranks, summed
+    over the splits that take the learned path (min(m, n) >= 24), as the device
+    path reported."""
+    model, *_ = trained
+    model.install()
+    rng = np.random.default_rng(8)
+    n, chi = 14, 64
+    mps, mpo = learned.laplacian_case(n, chi, rng)
+    kw = dict(tolerance=1e-12, max_bond_dimension=chi, max_sweeps=2, simplification_tolerance=0.0)
+    st = sg.DEFAULT_STRATEGY.replace(**kw)
+    sg.set_precision("mixed+learned")
+    _lib.stats_reset()
+    try:
+        with learned.record_truncations() as rec:
+            sg.MPO(mpo, st).apply(sg.MPS(mps), strategy=st)
+        stats = _lib.stats_read()
+    finally:
+        sg.set_precision("fp64")
+    k = np.round(np.exp2(rec.X[:, 35].astype(np.float64)))  # log2 min(m, n), stored in float32
+    take = k >= 24
+    r = np.clip(np.ceil(np.exp2(model.predict_log2(rec.X[take]).astype(np.float64))), 1, k[take])
+    assert stats["rank_predictions"] == int(take.sum()) > 5
+    # the feature logarithms are taken on the device there and on the host here: a
+    # last-bit difference may move a rank by one now and then
+    assert abs(stats["rank_predicted_sum"] - int(r.sum())) <= max(2, 0.002 * r.sum()), (
+        stats["rank_predicted_sum"], r.sum())
+
+
 def _workload_split(rng, m, n):
     """A numerically rank-deficient m x n matrix with the spectrum of the n=30, chi=256
     workload's splits: 256 values from 1 to 3e-3, two more near 2.5e-3, then zeros."""
