@@ -120,10 +120,6 @@ __device__ __forceinline__ void block_sum4(double& a, double& b, double& c, doub
 
 __device__ __forceinline__ void gamma_parts(double g, double& re, double& im) { re = g; im = 0.0; }
 __device__ __forceinline__ void gamma_parts(cplx g, double& re, double& im) { re = g.re; im = g.im; }
-__device__ __forceinline__ void make_coef(double& sp, double& sq, double s, double er, double ei) {
-  sp = s * er;  // real case: e = sign(gamma)
-  sq = s * er;
-}
 
 template <typename T> struct Rot;
 template <> struct Rot<double> {

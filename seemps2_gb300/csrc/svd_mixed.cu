@@ -148,13 +148,6 @@ __device__ __forceinline__ float f_im(float2 x) { return x.y; }
 __device__ __forceinline__ void f_set(float& x, float re, float) { x = re; }
 __device__ __forceinline__ void f_set(float2& x, float re, float im) { x = make_float2(re, im); }
 
-__device__ __forceinline__ float shfl_f(float x, int src) {
-  return __shfl_sync(0xffffffffu, x, src);
-}
-__device__ __forceinline__ float2 shfl_f(float2 x, int src) {
-  return make_float2(__shfl_sync(0xffffffffu, x.x, src), __shfl_sync(0xffffffffu, x.y, src));
-}
-
 // the elements of a float4 as F values
 __device__ __forceinline__ void unpack4(float4 t, float* v) {
   v[0] = t.x;
