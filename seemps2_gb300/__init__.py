@@ -36,6 +36,7 @@ from .core import (
     _update_right_environment,
     destructively_truncate_vector,
 )
+from . import hdf5
 from ._lib import set_precision
 from .operators import (CANONICALIZE_MPO, MPO, MPO_SIMPLIFICATION_STRATEGY, MPOList,
                         mpo_as_mps, mpo_scprod, mps_as_mpo, simplify_mpo)
