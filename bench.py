@@ -12,12 +12,17 @@ Reported (one JSON line on rank 0):
   value        sweeps/s with inputs resident in GPU memory (CUDA events)
   e2e          same through the public API from pinned host arrays, host<->device
                copies inside the timed region
+  phases       the step split into the MPO x MPS product, the canonical form
+               of the product and the state norm + sweeps (by difference), with
+               the sweep loop's own rate
   roofline     the dominant kernel: in the mixed forms the FP32 cluster
-               factorisation (latency bound; its FP32 rate against the SIMT
-               peak of its 16 SMs), else the dominant FP64 kernel (FP64 GEMM or
-               Jacobi SVD) against the FP64 peak measured in this run (the
-               library's FP64 GEMM; GB300 has no FP64 tensor path); plus the
-               FP64-accurate and 3xTF32 tensor-core products
+               factorisation (latency bound; the algorithmic SVD flops
+               4mn^2 + 8n^3 of its splits against the FP32 SIMT peak of the
+               whole GPU, the FP32 work as run beside it), else the dominant
+               FP64 kernel (FP64 GEMM or Jacobi SVD) against the FP64 peak
+               measured in this run (the library's FP64 GEMM; GB300 has no FP64
+               tensor path); plus the FP64-accurate and 3xTF32 tensor-core
+               products
   cpu_baseline the CPU oracle (NumPy/SciPy LAPACK, all host threads) on the
                same workload
 `--impl reference` times that CPU implementation alone, same workload.
@@ -176,6 +181,39 @@ def cpu_run(mps, mpo, chi, sweeps=2, want_result=False):
     res = so.mpo_apply(mpo, mps, st)
     dt = time.perf_counter() - t
     return (dt, res.sweeps, res) if want_result else (dt, res.sweeps)
+
+
+def phase_split(torch, sg, O, psi, st, step, flush, reps: int, sweeps: int) -> dict:
+    """Where one MPO.apply + simplify step spends its time, each phase timed on its own
+    with CUDA events (mean of `reps` runs, L2 flushed before each): the MPO x MPS
+    product, the canonical form of the product that starts the sweeps (centre 0, with
+    truncation, as the step runs it), and the rest of the step by difference: the state
+    norm from the factors and the sweeps.  `sweep_loop` is the sweep rate of that rest."""
+
+    def timed(fn):
+        ts, r = [], None
+        for _ in range(reps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return sum(ts) / len(ts), r
+
+    product_ms, prod = timed(lambda: O.apply(psi, strategy=st, simplify=False))
+    canon_ms, _ = timed(lambda: sg.CanonicalMPS(prod, center=0, normalize=False, strategy=st))
+    del prod
+    step_ms, _ = timed(step)
+    rest = step_ms - product_ms - canon_ms
+    return {"product_ms": product_ms, "canonical_form_ms": canon_ms,
+            "norm_and_sweeps_ms": rest, "step_ms": step_ms,
+            "sweep_loop": {"value": sweeps / (rest / 1e3) if rest > 0 else None,
+                           "unit": "sweeps/s", "sweeps": sweeps},
+            "method": "product and canonical form timed as separate calls; the state norm "
+                      "and the sweeps are the step minus both"}
 
 
 def run_reference(args):
@@ -806,6 +844,13 @@ def main():
         d2h = sum(t.numel() * t.element_size() for t in host)
     e2e_value = world * sweeps_per_step / statistics.mean(e2e_times)
 
+    # ---- phase split of the step ----------------------------------------------
+    try:
+        phases = phase_split(torch, sg, O, psi, st, step, flush, max(1, args.steps),
+                             sweeps_per_step)
+    except Exception as exc:  # a reporting extra must not hide the line
+        phases = {"failed": f"{type(exc).__name__}: {exc}"}
+
     # ---- roofline of the dominant kernel (one instrumented step) -----------
     _lib.stats_reset(timing=True)
     torch.cuda.synchronize()
@@ -929,7 +974,7 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches, "bonds_out": out.bond_dimensions()[: args.n // 2 + 1],
-            "error": out.error(), "oracle_check": oracle_check,
+            "error": out.error(), "oracle_check": oracle_check, "phases": phases,
         }
         if plain:
             line["plain_fp64"] = plain
