@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import warnings
 from collections.abc import Iterable, Sequence
 
 import numpy as np
@@ -134,7 +135,24 @@ class MPS(TensorArray):
     def conj(self) -> "MPS":
         return MPS([A.conj().resolve_conj() for A in self._data], self._error)
 
+    def reverse(self) -> "MPS":
+        """Sites in reverse order, each A[a, i, b] read as A[b, i, a] (state/mps.py:471-485;
+        like the reference, the result carries no error bound)."""
+        return MPS([A.permute(2, 1, 0).contiguous() for A in reversed(self._data)])
+
+    def to_tensor(self):
+        """The wavefunction as a tensor with one index per site (state/mps.py:103-106)."""
+        return self.to_vector().reshape(self.physical_dimensions())
+
+    def __copy__(self):
+        return self.copy()
+
     # --- scalars -----------------------------------------------------------
+    def norm2(self) -> float:
+        """Deprecated alias of `norm_squared` (state/mps.py:233-238)."""
+        warnings.warn("method norm2 is deprecated, use norm_squared", category=DeprecationWarning)
+        return self.norm_squared()
+
     def norm_squared(self) -> float:
         return abs(scprod(self, self).real)
 
@@ -473,6 +491,51 @@ class MPSSum:
 
     def to_vector(self):
         return sum(w * s.to_vector() for w, s in zip(self.weights, self.states))
+
+    def to_tensor(self):
+        return self.to_vector().reshape(self.physical_dimensions())
+
+    def __copy__(self):
+        return self.copy()
+
+    def conj(self) -> "MPSSum":
+        """Complex conjugate: conjugated weights and states (state/mpssum.py:173-177)."""
+        return MPSSum([w.conjugate() for w in self.weights], [s.conj() for s in self.states],
+                      check_args=False)
+
+    def reverse(self) -> "MPSSum":
+        """Every state with its sites reversed (state/mpssum.py:247-252)."""
+        return MPSSum(self.weights, [s.reverse() for s in self.states], check_args=False)
+
+    def delete_zero_components(self) -> float:
+        """Drop the terms whose weighted norm is zero and return the norm squared of
+        the sum over the rest (state/mpssum.py:204-228): terms are taken in order, each
+        kept term adds |w_i|^2 <s_i|s_i> and 2 Re(conj(w_i) w_j <s_i|s_j>) against the
+        terms kept before it; with no term left the sum becomes 0 * zero_state.  The
+        overlaps run on the device (the scprod kernel)."""
+        c = 0.0
+        weights: list = []
+        states: list = []
+        for wi, si in zip(self.weights, self.states):
+            wic = wi.conjugate()
+            ni = (wic * wi).real * si.norm_squared()
+            if ni:
+                for wj, sj in zip(weights, states):
+                    c += 2 * (wic * wj * scprod(si, sj)).real
+                weights.append(wi)
+                states.append(si)
+                c += ni
+        if len(weights) < len(self.states):
+            if not weights:
+                self.weights = [0.0]
+                self.states = [self.states[0].zero_state()]
+                return 0.0
+            self.weights, self.states = weights, states
+        return abs(float(c))
+
+    def join_canonical(self, *args, **kwargs) -> "CanonicalMPS":
+        """`join` followed by the canonical form (state/mpssum.py:169-171)."""
+        return CanonicalMPS(self.join(), *args, **kwargs)
 
     def join(self) -> MPS:
         """Block-diagonal join (state/mpssum.py:130-167)."""
