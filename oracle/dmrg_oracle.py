@@ -20,11 +20,13 @@ import numpy as np
 
 
 def contract_last_and_first(A, B):
+    """Last index of A against the first of B (cython/_python_core.py:220-227)."""
     return np.tensordot(A, B, axes=(-1, 0))
 
 
 def two_site_hamiltonian(O1, O2):
-    """H[c, ko, k, lo, l, d] of two neighbouring MPO sites O[c, i, j, e]."""
+    """H[c, ko, k, lo, l, d] of two neighbouring MPO sites O[c, i, j, e]
+    (the H12 of QuadraticForm.two_site_block, operators/quadratic.py:102-104)."""
     return contract_last_and_first(O1, O2)
 
 
@@ -58,6 +60,7 @@ def dense_operator(L, H, R):
 
 
 def begin_mpo_environment():
+    """The trivial 1 x 1 x 1 edge environment (state/environments.py:15-16)."""
     return np.ones((1, 1, 1))
 
 
@@ -76,7 +79,9 @@ def update_right_mpo_environment(rho, A, O, B):
 
 
 def heisenberg_mpo(n: int, J: float = 1.0):
-    """Open-chain spin-1/2 Heisenberg MPO, bond 5 (edges 1)."""
+    """Open-chain spin-1/2 Heisenberg MPO, bond 5 (edges 1): the operator of
+    HeisenbergHamiltonian(n).to_mpo() (hamiltonians/nearest_neighbor.py:318, :105-150),
+    checked against the reference-made heisenberg_mpo_L100.npz fixture."""
     Sp = np.array([[0.0, 1.0], [0.0, 0.0]])
     Sm = Sp.T
     Sz = np.diag([0.5, -0.5])

@@ -39,6 +39,8 @@ DEFAULT_TOLERANCE = float(np.finfo(np.float64).eps)
 
 
 class Truncation:
+    """Truncation method codes (cython/truncation.pxi:23-42)."""
+
     DO_NOT_TRUNCATE = 0
     RELATIVE_SINGULAR_VALUE = 1
     RELATIVE_NORM_SQUARED_ERROR = 2
@@ -46,6 +48,8 @@ class Truncation:
 
 
 class Simplification:
+    """Simplification method codes (cython/truncation.pxi:44-61)."""
+
     DO_NOT_SIMPLIFY = 0
     CANONICAL_FORM = 1
     VARIATIONAL = 2
@@ -370,7 +374,7 @@ def right_orth_2site(AA, strategy, rec=None, site=-1):
 
 
 class AntilinearForm:
-    """<bra|ket> with cached left/right environments."""
+    """<bra|ket> with cached left/right environments (state/antilinear.py:13-146)."""
 
     def __init__(self, bra: list, ket: list, center: int = 0):
         size = len(bra)

@@ -128,3 +128,39 @@ def test_dmrg_oracle_matches_reference_run():
     v = so.to_vector(state)
     ref = z["vector"].reshape(-1)
     assert 1.0 - abs(np.vdot(ref, v)) / (np.linalg.norm(ref) * np.linalg.norm(v)) <= 1e-8
+
+
+def _mpo_dense(W):
+    """Dense operator of an MPO O[a, i, j, b] (small chains only)."""
+    M = W[0][0]  # (i, j, b)
+    for O in W[1:]:
+        M = np.einsum("ijb,bklc->ikjlc", M, O)
+        n = M.shape[0] * M.shape[1]
+        M = M.reshape(n, n, -1)
+    return M[:, :, 0]
+
+
+def test_heisenberg_oracle_matches_reference_mpo():
+    """The oracle's Heisenberg MPO is the operator of the reference's
+    HeisenbergHamiltonian(100).to_mpo() (fixture heisenberg_mpo_L100.npz): the same
+    energy <psi|H|psi> for seeded random states on all 100 sites, and the same dense
+    operator on 6 sites built from the fixture's edge and bulk tensors."""
+    import os
+
+    from oracle import dmrg_oracle as do
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "heisenberg_mpo_L100.npz"))
+    ref = [z[f"W{i}"] for i in range(100)]
+    ours = do.heisenberg_mpo(100)
+    rng = np.random.default_rng(7)
+    for _ in range(3):
+        psi = [A / np.linalg.norm(A) for A in so.random_mps(2, 100, 3, rng)]
+        e = []
+        for W in (ref, ours):
+            L = do.begin_mpo_environment()
+            for A, O in zip(psi, W):
+                L = do.update_left_mpo_environment(L, A, O, A)
+            e.append(float(L.reshape(-1)[0]))
+        assert abs(e[0] - e[1]) <= 1e-12 * max(1.0, abs(e[0]))
+    small = [ref[0]] + [ref[1]] * 4 + [ref[99]]
+    assert np.allclose(_mpo_dense(small), _mpo_dense(do.heisenberg_mpo(6)), atol=1e-14)
